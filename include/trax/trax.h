@@ -1,0 +1,178 @@
+/* trax.h -- C ABI of the sm_103a triplet-seeding library (libtrax_gb300.so).
+ *
+ * Plain C types only: the caller passes host pointers and sizes, the library
+ * owns its device memory, stream and events.  Every call returns a status
+ * code (TRAX_OK == 0); trax_last_error() describes the last failure.
+ *
+ * Each entry point replaces one operator of the reference's triplet-seeding
+ * path (JuantAldea/trax, OpenCL).  The comment above each declaration names
+ * the reference interface it stands in for (file:line inside that project).
+ * In the reference those operators are C++ classes whose run() methods take
+ * clever:: OpenCL containers; here the containers live inside the context
+ * and run() becomes one call.
+ *
+ * Index conventions follow the reference: hit indices in results are
+ * positions in the grid-ordered hit collection (what GridBuilder::run leaves
+ * in the HitCollection, GridBuilder.cpp:151); trax_get_hit_perm maps them back
+ * to the caller's input order.
+ */
+#ifndef TRAX_H_
+#define TRAX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define TRAX_OK 0
+#define TRAX_ERR_CUDA 1          /* a CUDA runtime call failed */
+#define TRAX_ERR_ARG 2           /* invalid argument or input */
+#define TRAX_ERR_CAPACITY 3      /* a result does not fit the configured capacity */
+#define TRAX_ERR_TIMEOUT 4       /* a bounded device-side wait ran out */
+#define TRAX_ERR_DEVICE_ASSERT 5 /* a device-side bounds check fired */
+#define TRAX_ERR_STATE 6         /* call out of order (e.g. a stage before its input exists) */
+
+typedef struct trax_ctx trax_ctx;
+
+/* One row of the layer-triplet table: the 12 columns of
+ * TripletConfiguration.h:9-33 (configs/layerTriplets.xml). */
+typedef struct trax_layer_triplet {
+  uint32_t layer1, layer2, layer3;
+  float dtheta_cut;
+  float sigma_z;
+  float dphi_cut;
+  float sigma_phi;
+  float tip_cut;
+  uint32_t pair_spread_z;
+  float z0;
+  uint32_t pair_spread_phi;
+  uint32_t n_candidates;
+} trax_layer_triplet;
+
+/* The 7 SoA columns of HitCollection (HitCollection.h:23). */
+typedef struct trax_hits_soa {
+  const float* x;
+  const float* y;
+  const float* z;
+  const uint32_t* layer;  /* 1-based detector layer */
+  const uint32_t* det_id;
+  const uint32_t* hit_id; /* simulated track id */
+  const uint32_t* event;  /* event number inside the batch */
+} trax_hits_soa;
+
+/* Options of the batched call. */
+typedef struct trax_batch_opts {
+  int use_graph;        /* capture the chain in a CUDA graph and replay it */
+  int run_linking;      /* 1: connectivity, circle fit and CA; 0: stop after the filter */
+  float d_eta_cut;      /* TripletConnectivityTight dEtaCut (TripletBuilder.cpp:793: 0.0256) */
+} trax_batch_opts;
+
+/* Sizes produced by the last chain run. */
+typedef struct trax_batch_stats {
+  uint64_t n_hits;
+  uint64_t n_pairs;
+  uint64_t n_candidates;
+  uint64_t n_triplets;
+  uint64_t n_links;
+  uint64_t n_connectable;
+  uint64_t n_non_connectable;
+  uint64_t n_track_entries;
+  uint64_t n_pair_sentinels;      /* pair slots the reference leaves unwritten */
+  uint64_t n_candidate_sentinels; /* candidate slots the reference leaves unwritten */
+  uint64_t kernel_launches;       /* kernels launched by the last run */
+  double device_ms;               /* device time of the last run (CUDA events) */
+} trax_batch_stats;
+
+/* ---------------------------------------------------------------- context
+ * Replaces clever::context creation (TripletBuilder.cpp:66-129).
+ * One context per host thread; it owns a CUDA stream and its buffers. */
+int trax_create(trax_ctx** ctx, int device);
+void trax_destroy(trax_ctx* ctx);
+const char* trax_last_error(const trax_ctx* ctx);
+const char* trax_version(void);
+
+/* ---------------------------------------------------------- configuration
+ * TripletConfigurations + minRadiusCurvature (TripletConfiguration.h:39-72,
+ * TripletConfiguration.cpp:36-43).  Row p must have layer1 == p + 1 (the
+ * reference derives the layer-triplet index from the first hit's layer,
+ * TripletThetaPhiPredictor.h:88). */
+int trax_set_layer_triplets(trax_ctx* ctx, const trax_layer_triplet* lt, int n, float min_pt);
+
+/* GeometrySupplement (GeometrySupplement.h:21-43): min/max radius of layers 1..n. */
+int trax_set_geometry(trax_ctx* ctx, const float* min_r, const float* max_r, int n_layers);
+
+/* GridConfig (Grid.h:5-39): z range fixed to [-300, 300] cm, phi to [-pi, pi]. */
+int trax_set_grid(trax_ctx* ctx, uint32_t n_z, uint32_t n_phi);
+
+/* HitCollection + EventSupplement + LayerSupplement upload
+ * (TripletBuilder.cpp:296-307; HitCollection.cpp:120-163 layout).
+ * Hits are sorted by event, then layer; layer_hits/layer_offsets are
+ * [n_events * n_layers], offsets relative to the event's first hit. */
+int trax_upload_hits(trax_ctx* ctx, const trax_hits_soa* hits, uint32_t n_hits,
+                     const uint32_t* event_offsets, const uint32_t* layer_hits,
+                     const uint32_t* layer_offsets, uint32_t n_events, uint32_t n_layers);
+
+/* ------------------------------------------------------ stage by stage
+ * GridBuilder::run (GridBuilder.h:42, GridBuilder.cpp:6-161): per-(event,
+ * layer) z/phi grid and the grid-ordered hit collection. */
+int trax_grid_build(trax_ctx* ctx);
+
+/* PairGeneratorBeamspot::run (PairGeneratorBeamspot.h:40-41, .cpp:5-183). */
+int trax_pair_gen(trax_ctx* ctx, uint64_t* n_pairs);
+
+/* TripletThetaPhiPredictor::run (TripletThetaPhiPredictor.h:44-47, .cpp:10-168). */
+int trax_triplet_predict(trax_ctx* ctx, uint64_t* n_candidates);
+
+/* TripletThetaPhiFilter::run (TripletThetaPhiFilter.h:46-48, .cpp:10-206). */
+int trax_triplet_filter(trax_ctx* ctx, uint64_t* n_triplets);
+
+/* TripletConnectivityTight::run (TripletConnectivityTight.h:42-44, .cpp:5-475). */
+int trax_connectivity(trax_ctx* ctx, float d_eta_cut, uint64_t* n_links);
+
+/* TrackletCircleFitter::run (TrackletCircleFitter.h:25-29, .cpp:3-49). */
+int trax_circle_fit(trax_ctx* ctx);
+
+/* CellularAutomaton::run (CellularAutomaton.h:43-49, .cpp:7-465). */
+int trax_cellular_automaton(trax_ctx* ctx, uint64_t* n_track_entries);
+
+/* PrefixSum::run (PrefixSum.h:43-44, PrefixSum.cpp:8-36): exclusive uint32
+ * scan of `n` elements of the host array `data` in place (round trip through
+ * the device; single-pass decoupled-lookback scan). */
+int trax_prefix_sum(trax_ctx* ctx, uint32_t* data, uint64_t n);
+
+/* ------------------------------------------------------------- batched
+ * The whole chain (buildTriplets, TripletBuilder.cpp:312-467) for all
+ * uploaded events in one pass of batched launches, optionally replayed from a
+ * CUDA graph. */
+int trax_seed_batch(trax_ctx* ctx, const trax_batch_opts* opts, trax_batch_stats* stats);
+
+/* ------------------------------------------------------------- results
+ * Sizes first (*_size), then copies into caller-allocated host buffers. */
+int trax_get_stats(trax_ctx* ctx, trax_batch_stats* stats);
+/* Pairing::pairing / pairingOffsets (Pairings.h:9-59): pairs as (inner, outer)
+ * uint32 pairs, offsets [n_events * n_lt + 1]. */
+int trax_get_pairs(trax_ctx* ctx, uint32_t* pairs2, uint32_t* offsets);
+/* Candidates (pair index, third hit) and their offsets. */
+int trax_get_candidates(trax_ctx* ctx, uint32_t* cands2, uint32_t* offsets);
+/* TrackletCollection hit columns and trackletOffsets (TrackletCollection.h:32-78). */
+int trax_get_triplets(trax_ctx* ctx, uint32_t* h1, uint32_t* h2, uint32_t* h3, uint32_t* offsets);
+/* Per-triplet eta (TripletConnectivityTight.h:47-79) and circle radius (TrackletCircleFitter.h:97). */
+int trax_get_triplet_eta_pt(trax_ctx* ctx, float* eta, float* pt);
+/* Links (basis, follower) and connectable / non-connectable index lists. */
+int trax_get_links(trax_ctx* ctx, uint32_t* basis, uint32_t* follower, uint32_t* connectable,
+                   uint32_t* non_connectable);
+/* CA states, track collection and its offsets [n_triplets + 1]. */
+int trax_get_tracks(trax_ctx* ctx, uint32_t* states, uint32_t* tracks, uint32_t* track_offsets);
+/* Grid boundaries [n_events * n_layers * (n_z+1)(n_phi+1)] and, for every
+ * grid-ordered hit, its index in the uploaded input. */
+int trax_get_grid(trax_ctx* ctx, uint32_t* grid, uint64_t* n_cells);
+int trax_get_hit_perm(trax_ctx* ctx, uint32_t* perm);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TRAX_H_ */

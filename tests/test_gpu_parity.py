@@ -1,0 +1,160 @@
+"""GPU parity: the sm_103a chain, called through the C ABI, against the CPU oracle.
+
+Every stage output is compared exactly (integer arrays element by element,
+float arrays bit for bit): the FP32 cut predicates use the same math in the
+same operation order on both sides, so exact equality is the bar.
+"""
+import numpy as np
+import pytest
+
+from trax_gb300 import events
+
+pytestmark = pytest.mark.gpu
+
+INT_ARRAYS = ["perm", "grid", "pairs", "pair_offsets", "cands", "cand_offsets", "trip_h1", "trip_h2", "trip_h3",
+              "trip_offsets", "link_basis", "link_follower", "connectable", "non_connectable", "ca_states", "tracks",
+              "track_offsets"]
+FLOAT_ARRAYS = ["eta", "pt"]
+
+
+def compare(got, ref, names=None):
+    bad = []
+    for name in names or (INT_ARRAYS + FLOAT_ARRAYS):
+        if name not in ref:
+            continue
+        a, b = np.asarray(got[name]), np.asarray(ref[name])
+        if name in FLOAT_ARRAYS:
+            a, b = a.view(np.uint32), b.view(np.uint32)
+        if a.shape != b.shape:
+            bad.append(f"{name}: shape {a.shape} vs oracle {b.shape}")
+        elif not np.array_equal(a, b):
+            idx = np.nonzero(a != b)[0]
+            bad.append(f"{name}: {idx.size} differences, first at {idx[0]}: {a[idx[0]]} vs {b[idx[0]]}")
+    assert not bad, "; ".join(bad)
+
+
+def stagewise(ctx, batch):
+    ctx.upload(batch)
+    ctx.grid_build()
+    ctx.pair_gen()
+    ctx.triplet_predict()
+    ctx.triplet_filter()
+    n_links = ctx.connectivity(batch.d_eta_cut)
+    if n_links:
+        ctx.circle_fit()
+        ctx.cellular_automaton()
+    return ctx.results()
+
+
+@pytest.fixture(scope="module")
+def ctx(trax_lib):
+    c = trax_lib.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("config", [0, 1])
+def test_stagewise_matches_oracle(ctx, oracle_lib, config):
+    batch = events.generate(config)
+    ref = oracle_lib.run(batch)[0]
+    got = stagewise(ctx, batch)
+    compare(got, ref)
+    assert got["trip_h1"].size > 0
+
+
+@pytest.mark.parametrize("config,n_events", [(1, 100), (2, 6)])
+def test_batched_graph_matches_oracle(ctx, oracle_lib, config, n_events):
+    batch = events.generate(config, n_events=n_events)
+    ref = oracle_lib.run(batch)[0]
+    ctx.upload(batch)
+    stats = ctx.seed_batch(use_graph=True)
+    got = ctx.results()
+    compare(got, ref)
+    assert stats.n_triplets == ref["trip_h1"].size
+    assert stats.n_links == ref["link_basis"].size
+    # a second replay of the captured graph gives the same arrays
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
+def test_batched_synced_matches_graph(ctx, oracle_lib):
+    batch = events.generate(2, n_events=4)
+    ctx.upload(batch)
+    ctx.seed_batch(use_graph=False)
+    a = ctx.results()
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), a)
+
+
+def test_empty_layers_and_events(ctx, oracle_lib):
+    batch = events.generate(1, n_events=5)
+    # drop every hit of event 2 and of layer 3 in event 4
+    keep = np.ones(batch.n_hits, dtype=bool)
+    keep[batch.event == 2] = False
+    keep[(batch.event == 4) & (batch.layer == 3)] = False
+    lh = batch.layer_hits.copy()
+    lh[2, :] = 0
+    lh[4, 2] = 0
+    sub = events._assemble({k: getattr(batch, k)[keep] for k in ("x", "y", "z", "layer", "det_id", "hit_id", "event")},
+                           lh, batch)
+    ref = oracle_lib.run(sub)[0]
+    ctx.upload(sub)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
+def test_single_event_single_track(ctx, oracle_lib):
+    batch = events.generate(0, n_events=1)
+    ref = oracle_lib.run(batch)[0]
+    got = stagewise(ctx, batch)
+    compare(got, ref)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 2047, 2048, 2049, 123457, 4 * 1024 * 1024 + 3])
+def test_prefix_sum_random(ctx, n):
+    rng = np.random.default_rng(n)
+    x = rng.integers(0, 1000, n, dtype=np.uint32)
+    got = ctx.prefix_sum(x)
+    ref = np.concatenate([[0], np.cumsum(x, dtype=np.uint64)[:-1]]).astype(np.uint32)
+    assert np.array_equal(got, ref)
+
+
+def test_prefix_sum_all_ones_kat(ctx):
+    # trax_test.cpp:437-479: scanning 1 Mi ones must leave SIZE-1 in the last slot
+    size = 1024 * 1024
+    out = ctx.prefix_sum(np.ones(size, dtype=np.uint32))
+    assert out[size - 1] == size - 1
+
+
+def test_prefix_sum_wraps_like_uint32(ctx):
+    x = np.full(10, 0x80000000, dtype=np.uint32)
+    out = ctx.prefix_sum(x)
+    assert out.tolist() == [(k * 0x80000000) & 0xffffffff for k in range(10)]
+
+
+def test_stage_order_is_enforced(trax_lib):
+    with trax_lib.Context(0) as c:
+        batch = events.generate(0, n_events=2)
+        c.upload(batch)
+        with pytest.raises(trax_lib.TraxError) as e:
+            c.pair_gen()
+        assert e.value.code == 6
+
+
+def test_invalid_layer_triplets_rejected(trax_lib):
+    with trax_lib.Context(0) as c:
+        batch = events.generate(0, n_events=1)
+        bad = [events.LayerTriplet(2, 3, 4, 0.01, 0.037, 0.05, 0.032, 1.0, 2, 10.0, 2, 4)]
+        with pytest.raises(trax_lib.TraxError) as e:
+            c.set_layer_triplets(bad, batch.min_pt)
+        assert e.value.code == 2
+
+
+def test_hits_outside_grid_rejected(trax_lib):
+    with trax_lib.Context(0) as c:
+        batch = events.generate(0, n_events=1)
+        batch.z[0] = np.float32(450.0)
+        c.upload(batch)
+        with pytest.raises(trax_lib.TraxError) as e:
+            c.grid_build()
+        assert e.value.code == 5

@@ -1,0 +1,344 @@
+"""ctypes binding of the C ABI in include/trax/trax.h (libtrax_gb300.so).
+
+This is the Python view of the same entry points a C, C++ or cgo caller
+binds.  The library must have been built (``trax_gb300.build.build()`` or
+``__graft_entry__.build()``); loading fails loudly otherwise -- there is no
+fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+import threading
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import build as _build
+
+TRAX_OK = 0
+ERRORS = {1: "TRAX_ERR_CUDA", 2: "TRAX_ERR_ARG", 3: "TRAX_ERR_CAPACITY", 4: "TRAX_ERR_TIMEOUT",
+          5: "TRAX_ERR_DEVICE_ASSERT", 6: "TRAX_ERR_STATE"}
+
+EXPORTED = [
+    "trax_create", "trax_destroy", "trax_last_error", "trax_version", "trax_set_layer_triplets",
+    "trax_set_geometry", "trax_set_grid", "trax_upload_hits", "trax_grid_build", "trax_pair_gen",
+    "trax_triplet_predict", "trax_triplet_filter", "trax_connectivity", "trax_circle_fit",
+    "trax_cellular_automaton", "trax_prefix_sum", "trax_seed_batch", "trax_get_stats", "trax_get_pairs",
+    "trax_get_candidates", "trax_get_triplets", "trax_get_triplet_eta_pt", "trax_get_links",
+    "trax_get_tracks", "trax_get_grid", "trax_get_hit_perm",
+]
+
+
+class TraxError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class LayerTripletC(ctypes.Structure):
+    _fields_ = [("layer1", ctypes.c_uint32), ("layer2", ctypes.c_uint32), ("layer3", ctypes.c_uint32),
+                ("dtheta_cut", ctypes.c_float), ("sigma_z", ctypes.c_float), ("dphi_cut", ctypes.c_float),
+                ("sigma_phi", ctypes.c_float), ("tip_cut", ctypes.c_float),
+                ("pair_spread_z", ctypes.c_uint32), ("z0", ctypes.c_float),
+                ("pair_spread_phi", ctypes.c_uint32), ("n_candidates", ctypes.c_uint32)]
+
+
+class HitsSoaC(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("layer", ctypes.c_void_p), ("det_id", ctypes.c_void_p), ("hit_id", ctypes.c_void_p),
+                ("event", ctypes.c_void_p)]
+
+
+class BatchOptsC(ctypes.Structure):
+    _fields_ = [("use_graph", ctypes.c_int), ("run_linking", ctypes.c_int), ("d_eta_cut", ctypes.c_float)]
+
+
+class BatchStatsC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in (
+        "n_hits", "n_pairs", "n_candidates", "n_triplets", "n_links", "n_connectable", "n_non_connectable",
+        "n_track_entries", "n_pair_sentinels", "n_candidate_sentinels", "kernel_launches")] + [
+        ("device_ms", ctypes.c_double)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    """Load libtrax_gb300.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build() (there is no CPU fallback)")
+        L = ctypes.CDLL(path)
+        vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+        pu64 = ctypes.POINTER(ctypes.c_uint64)
+        sig = {
+            "trax_create": ([ctypes.POINTER(vp), i32], i32),
+            "trax_destroy": ([vp], None),
+            "trax_last_error": ([vp], ctypes.c_char_p),
+            "trax_version": ([], ctypes.c_char_p),
+            "trax_set_layer_triplets": ([vp, vp, i32, ctypes.c_float], i32),
+            "trax_set_geometry": ([vp, vp, vp, i32], i32),
+            "trax_set_grid": ([vp, u32, u32], i32),
+            "trax_upload_hits": ([vp, vp, u32, vp, vp, vp, u32, u32], i32),
+            "trax_grid_build": ([vp], i32),
+            "trax_pair_gen": ([vp, pu64], i32),
+            "trax_triplet_predict": ([vp, pu64], i32),
+            "trax_triplet_filter": ([vp, pu64], i32),
+            "trax_connectivity": ([vp, ctypes.c_float, pu64], i32),
+            "trax_circle_fit": ([vp], i32),
+            "trax_cellular_automaton": ([vp, pu64], i32),
+            "trax_prefix_sum": ([vp, vp, u64], i32),
+            "trax_seed_batch": ([vp, vp, vp], i32),
+            "trax_get_stats": ([vp, vp], i32),
+            "trax_get_pairs": ([vp, vp, vp], i32),
+            "trax_get_candidates": ([vp, vp, vp], i32),
+            "trax_get_triplets": ([vp, vp, vp, vp, vp], i32),
+            "trax_get_triplet_eta_pt": ([vp, vp, vp], i32),
+            "trax_get_links": ([vp, vp, vp, vp, vp], i32),
+            "trax_get_tracks": ([vp, vp, vp, vp], i32),
+            "trax_get_grid": ([vp, vp, pu64], i32),
+            "trax_get_hit_perm": ([vp, vp], i32),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+        return L
+
+
+def _p(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+@dataclasses.dataclass
+class BatchStats:
+    n_hits: int
+    n_pairs: int
+    n_candidates: int
+    n_triplets: int
+    n_links: int
+    n_connectable: int
+    n_non_connectable: int
+    n_track_entries: int
+    n_pair_sentinels: int
+    n_candidate_sentinels: int
+    kernel_launches: int
+    device_ms: float
+
+
+class Context:
+    """One trax_ctx: a CUDA stream and the device buffers of one batch."""
+
+    def __init__(self, device: int = 0):
+        self._L = load()
+        h = ctypes.c_void_p()
+        rc = self._L.trax_create(ctypes.byref(h), device)
+        if rc != TRAX_OK:
+            raise TraxError(rc, "trax_create failed (no usable CUDA device?)")
+        self._h = h
+        self._keep = []
+        self.n_lt = 0
+        self.n_events = 0
+        self.n_layers = 0
+        self.n_hits = 0
+        self.n_z = 0
+        self.n_phi = 0
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, rc: int):
+        if rc != TRAX_OK:
+            raise TraxError(rc, self._L.trax_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.trax_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -------------------------------------------------------- configuration
+    def set_layer_triplets(self, lts, min_pt: float):
+        arr = (LayerTripletC * len(lts))()
+        for i, lt in enumerate(lts):
+            for f in LayerTripletC._fields_:
+                setattr(arr[i], f[0], getattr(lt, f[0]))
+        self._check(self._L.trax_set_layer_triplets(self._h, ctypes.cast(arr, ctypes.c_void_p), len(lts), min_pt))
+        self.n_lt = len(lts)
+
+    def set_geometry(self, min_r: np.ndarray, max_r: np.ndarray):
+        a = np.ascontiguousarray(min_r, dtype=np.float32)
+        b = np.ascontiguousarray(max_r, dtype=np.float32)
+        self._check(self._L.trax_set_geometry(self._h, _p(a), _p(b), a.size))
+
+    def set_grid(self, n_z: int, n_phi: int):
+        self._check(self._L.trax_set_grid(self._h, n_z, n_phi))
+        self.n_z, self.n_phi = n_z, n_phi
+
+    def upload(self, batch):
+        """Configuration and hits of an EventBatch (trax_gb300.events)."""
+        self.set_layer_triplets(batch.lts, batch.min_pt)
+        self.set_geometry(batch.min_r, batch.max_r)
+        self.set_grid(batch.n_z, batch.n_phi)
+        self.upload_hits(batch)
+
+    def upload_hits(self, batch):
+        cols = [np.ascontiguousarray(getattr(batch, k), dtype=dt) for k, dt in (
+            ("x", np.float32), ("y", np.float32), ("z", np.float32), ("layer", np.uint32),
+            ("det_id", np.uint32), ("hit_id", np.uint32), ("event", np.uint32))]
+        soa = HitsSoaC(*[_p(c) for c in cols])
+        eo = np.ascontiguousarray(batch.event_offsets, dtype=np.uint32)
+        lh = np.ascontiguousarray(batch.layer_hits.reshape(-1), dtype=np.uint32)
+        lo = np.ascontiguousarray(batch.layer_offsets.reshape(-1), dtype=np.uint32)
+        self._check(self._L.trax_upload_hits(self._h, ctypes.byref(soa), batch.n_hits, _p(eo), _p(lh), _p(lo),
+                                             batch.n_events, batch.n_layers))
+        self.n_events, self.n_layers, self.n_hits = batch.n_events, batch.n_layers, batch.n_hits
+
+    # --------------------------------------------------------------- stages
+    def grid_build(self):
+        self._check(self._L.trax_grid_build(self._h))
+
+    def _count(self, fn, *args) -> int:
+        n = ctypes.c_uint64()
+        self._check(fn(self._h, *args, ctypes.byref(n)))
+        return int(n.value)
+
+    def pair_gen(self) -> int:
+        return self._count(self._L.trax_pair_gen)
+
+    def triplet_predict(self) -> int:
+        return self._count(self._L.trax_triplet_predict)
+
+    def triplet_filter(self) -> int:
+        return self._count(self._L.trax_triplet_filter)
+
+    def connectivity(self, d_eta_cut: float) -> int:
+        return self._count(self._L.trax_connectivity, ctypes.c_float(d_eta_cut))
+
+    def circle_fit(self):
+        self._check(self._L.trax_circle_fit(self._h))
+
+    def cellular_automaton(self) -> int:
+        return self._count(self._L.trax_cellular_automaton)
+
+    def seed_batch(self, use_graph: bool = True, run_linking: bool = True, d_eta_cut: float = 0.0256) -> BatchStats:
+        opts = BatchOptsC(int(use_graph), int(run_linking), d_eta_cut)
+        st = BatchStatsC()
+        self._check(self._L.trax_seed_batch(self._h, ctypes.byref(opts), ctypes.byref(st)))
+        return BatchStats(*[getattr(st, f[0]) for f in BatchStatsC._fields_])
+
+    def stats(self) -> BatchStats:
+        st = BatchStatsC()
+        self._check(self._L.trax_get_stats(self._h, ctypes.byref(st)))
+        return BatchStats(*[getattr(st, f[0]) for f in BatchStatsC._fields_])
+
+    def prefix_sum(self, data: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(data, dtype=np.uint32).copy()
+        self._check(self._L.trax_prefix_sum(self._h, _p(a), a.size))
+        return a
+
+    # -------------------------------------------------------------- results
+    def _n_offsets(self) -> int:
+        return self.n_events * self.n_lt + 1
+
+    def pairs(self):
+        s = self.stats()
+        p = np.zeros((max(s.n_pairs, 1), 2), dtype=np.uint32)
+        o = np.zeros(self._n_offsets(), dtype=np.uint32)
+        self._check(self._L.trax_get_pairs(self._h, _p(p), _p(o)))
+        return p[:s.n_pairs], o
+
+    def candidates(self):
+        s = self.stats()
+        c = np.zeros((max(s.n_candidates, 1), 2), dtype=np.uint32)
+        o = np.zeros(self._n_offsets(), dtype=np.uint32)
+        self._check(self._L.trax_get_candidates(self._h, _p(c), _p(o)))
+        return c[:s.n_candidates], o
+
+    def triplets(self):
+        s = self.stats()
+        n = max(s.n_triplets, 1)
+        h1, h2, h3 = (np.zeros(n, dtype=np.uint32) for _ in range(3))
+        o = np.zeros(self._n_offsets(), dtype=np.uint32)
+        self._check(self._L.trax_get_triplets(self._h, _p(h1), _p(h2), _p(h3), _p(o)))
+        k = s.n_triplets
+        return h1[:k], h2[:k], h3[:k], o
+
+    def eta_pt(self):
+        s = self.stats()
+        n = max(s.n_triplets, 1)
+        eta, pt = np.zeros(n, dtype=np.float32), np.zeros(n, dtype=np.float32)
+        self._check(self._L.trax_get_triplet_eta_pt(self._h, _p(eta), _p(pt)))
+        return eta[:s.n_triplets], pt[:s.n_triplets]
+
+    def links(self):
+        s = self.stats()
+        b = np.zeros(max(s.n_links, 1), dtype=np.uint32)
+        f = np.zeros(max(s.n_links, 1), dtype=np.uint32)
+        c = np.zeros(max(s.n_connectable, 1), dtype=np.uint32)
+        nc = np.zeros(max(s.n_non_connectable, 1), dtype=np.uint32)
+        self._check(self._L.trax_get_links(self._h, _p(b), _p(f), _p(c), _p(nc)))
+        return b[:s.n_links], f[:s.n_links], c[:s.n_connectable], nc[:s.n_non_connectable]
+
+    def tracks(self):
+        s = self.stats()
+        states = np.zeros(max(s.n_triplets, 1), dtype=np.uint32)
+        tr = np.zeros(max(s.n_track_entries, 1), dtype=np.uint32)
+        off = np.zeros(s.n_triplets + 1, dtype=np.uint32)
+        self._check(self._L.trax_get_tracks(self._h, _p(states), _p(tr), _p(off)))
+        if s.n_links == 0:
+            return states[:0], tr[:0], off[:0]
+        return states[:s.n_triplets], tr[:s.n_track_entries], off
+
+    def grid(self) -> np.ndarray:
+        n = ctypes.c_uint64()
+        self._check(self._L.trax_get_grid(self._h, None, ctypes.byref(n)))
+        g = np.zeros(max(n.value, 1), dtype=np.uint32)
+        self._check(self._L.trax_get_grid(self._h, _p(g), ctypes.byref(n)))
+        return g[:n.value]
+
+    def hit_perm(self) -> np.ndarray:
+        p = np.zeros(max(self.n_hits, 1), dtype=np.uint32)
+        self._check(self._L.trax_get_hit_perm(self._h, _p(p)))
+        return p[:self.n_hits]
+
+    def results(self) -> Dict[str, np.ndarray]:
+        """All stage outputs in the oracle's naming."""
+        out = {"perm": self.hit_perm(), "grid": self.grid()}
+        p, po = self.pairs()
+        out["pairs"], out["pair_offsets"] = p.reshape(-1), po
+        c, co = self.candidates()
+        out["cands"], out["cand_offsets"] = c.reshape(-1), co
+        h1, h2, h3, to = self.triplets()
+        out.update(trip_h1=h1, trip_h2=h2, trip_h3=h3, trip_offsets=to)
+        s = self.stats()
+        if True:
+            eta, pt = self.eta_pt()
+            # without links the reference stops before the circle fit
+            out["eta"], out["pt"] = eta, (pt if s.n_links else pt[:0])
+            b, f, cn, nc = self.links()
+            out.update(link_basis=b, link_follower=f, connectable=cn, non_connectable=nc)
+            st, tr, toff = self.tracks()
+            out.update(ca_states=st, tracks=tr, track_offsets=toff)
+        return out

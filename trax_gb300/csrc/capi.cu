@@ -1,0 +1,1006 @@
+// capi.cu -- the C ABI of include/trax/trax.h: context, configuration,
+// uploads, the stage chain and result downloads.
+//
+// One chain implementation runs in two modes:
+//   * SYNCED: after every compaction scan the host reads the total (one
+//     4-byte device-to-host copy) and sizes the next buffers exactly -- the
+//     launch structure of the reference's run() methods (count, scan,
+//     downloadScalar, allocate, store).  The stage entry points use it.
+//   * DEVICE: no host reads.  Every kernel takes its item count from a fixed
+//     device slot (written by a one-thread publish kernel after each scan) and
+//     every output has a capacity learnt from an earlier SYNCED run plus
+//     headroom.  A total above its capacity is clamped and reported as
+//     TRAX_ERR_CAPACITY, never silently truncated.  This mode is captured once
+//     into a CUDA graph and replayed by trax_seed_batch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/trax/trax.h"
+#include "trax_kernels.h"
+
+using namespace trax;
+
+namespace trax {
+
+int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+}  // namespace trax
+
+namespace {
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+template <typename T>
+T* ptr(const DevBuf& b) {
+  return static_cast<T*>(b.p);
+}
+
+// fixed device slots of the error word, counters and totals
+enum Slot {
+  S_ERR = 0,
+  S_PAIR_SENT,
+  S_CAND_SENT,
+  S_TASKS,
+  S_PAIRS,
+  S_CANDS,
+  S_TRIPLETS,
+  S_LINKS,
+  S_CONN,
+  S_NONCONN,
+  S_TRACKS,
+  S_N
+};
+
+enum Mode { SYNCED, DEVICE };
+
+const uint64_t NO_CAP = 0xffffffffull;
+
+}  // namespace
+
+struct trax_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::string err;
+  // configuration
+  std::vector<trax_layer_triplet> lts;
+  float minPt = 0.0f;
+  std::vector<float> minR, maxR;
+  uint32_t nZ = 0, nP = 0;
+  bool haveLT = false, haveGeom = false, haveGrid = false, haveHits = false;
+  // batch shape
+  uint32_t E = 0, L = 0, nHits = 0;
+  float dEtaCut = 0.0256f;
+  DevConfig cfg;
+  // inputs
+  DevBuf in_x, in_y, in_z, in_layer, in_det, in_hid, in_evt, evOff, layHits, layOff;
+  // grid stage
+  DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
+  // pair stage
+  DevBuf segOuter, taskBase, taskCount, pairs, pairOffsets;
+  // prediction / filter
+  DevBuf candCount, cands, candOffsets, flags, h1, h2, h3, tripOffsets;
+  // connectivity / fit / CA
+  DevBuf eta, segOf, segStart, linkCount, cflags, basis, follower, connS, nonConnS, connIdx, nonConnIdx, pt;
+  DevBuf states, inStart, inCursor, inList, best, isBest, handlers, tracks;
+  // bookkeeping
+  DevBuf scanScratch, slots;
+  uint32_t* hSlots = nullptr;  // pinned copy of the slots
+  // sizes of the last run
+  uint64_t nTasks = 0, nPairs = 0, nCands = 0, nT = 0, nLinks = 0, nConn = 0, nNonConn = 0, nTracks = 0;
+  uint64_t pairSent = 0, candSent = 0;
+  int stage = 0;  // last completed stage: 1 grid .. 7 CA
+  bool noLinks = true;
+  uint32_t launches = 0;
+  // DEVICE-mode capacities and the captured graph
+  uint64_t capTasks = 0, capPairs = 0, capCands = 0, capT = 0, capLinks = 0, capTracks = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graphExec = nullptr;
+  uint64_t graphKey = 0;
+  uint64_t bufGeneration = 0;
+  uint32_t graphLaunches = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double lastMs = 0.0;
+};
+
+namespace {
+
+const char* kVersion = "trax_gb300 0.1 (sm_103a)";
+
+int fail(trax_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(trax_ctx* c, cudaError_t e, const char* where) {
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  return fail(c, TRAX_ERR_CUDA, m);
+}
+
+#define CK(call)                                           \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+  } while (0)
+
+#define RC(call)              \
+  do {                        \
+    int r_ = (call);          \
+    if (r_ != TRAX_OK) return r_; \
+  } while (0)
+
+cudaError_t ensure(trax_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (bytes <= b.cap) return cudaSuccess;
+  if (b.p) {
+    cudaError_t e = cudaFree(b.p);
+    if (e != cudaSuccess) return e;
+    b.p = nullptr;
+    b.cap = 0;
+  }
+  size_t want = bytes + bytes / 8 + 256;
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    b.p = nullptr;
+    return e;
+  }
+  b.cap = want;
+  c->bufGeneration++;
+  return cudaSuccess;
+}
+
+void release(DevBuf& b) {
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+}
+
+DevHits dev_hits(trax_ctx* c) {
+  DevHits h;
+  h.x = ptr<float>(c->px);
+  h.y = ptr<float>(c->py);
+  h.z = ptr<float>(c->pz);
+  h.layer = ptr<uint32_t>(c->player);
+  h.det = ptr<uint32_t>(c->pdet);
+  h.hid = ptr<uint32_t>(c->phid);
+  h.evt = ptr<uint32_t>(c->pevt);
+  h.orig = ptr<uint32_t>(c->porig);
+  h.xyzp = ptr<float4>(c->pxyzp);
+  return h;
+}
+
+uint32_t* slot(trax_ctx* c, int k) { return ptr<uint32_t>(c->slots) + k; }
+uint32_t* dev_err(trax_ctx* c) { return slot(c, S_ERR); }
+
+float min_radius_curvature(float minPt) {
+  // TripletConfiguration.cpp:36-43 with IDEAL_BZ = 3.8112 (TripletConfiguration.h:70)
+  const double IDEAL_BZ = 3.8112;
+  const double Q = 1.602177E-19;
+  const double GEV_C = 5.344286E-19;
+  return (float)(minPt * GEV_C / (IDEAL_BZ * Q) * 1E2);
+}
+
+int build_config(trax_ctx* c) {
+  if (!c->haveLT || !c->haveGeom || !c->haveGrid || !c->haveHits)
+    return fail(c, TRAX_ERR_STATE, "layer triplets, geometry, grid and hits must be set first");
+  DevConfig& g = c->cfg;
+  memset(&g, 0, sizeof(g));
+  g.E = c->E;
+  g.L = c->L;
+  g.nZ = c->nZ;
+  g.nP = c->nP;
+  g.C = (c->nZ + 1) * (c->nP + 1);
+  g.nLT = (uint32_t)c->lts.size();
+  // Grid.h:9-15, 33-37 (float arithmetic on the host)
+  const float MIN_Z = -300.0f, MAX_Z = 300.0f;
+  const float MIN_PHI = (float)-3.14159265358979323846, MAX_PHI = (float)3.14159265358979323846;
+  g.minZ = MIN_Z;
+  g.sZ = (MAX_Z - MIN_Z) / (float)c->nZ;
+  g.minPhi = MIN_PHI;
+  g.sP = (MAX_PHI - MIN_PHI) / (float)c->nP;
+  g.minRcurv = min_radius_curvature(c->minPt);
+  g.dEtaCut = c->dEtaCut;
+  for (uint32_t p = 0; p < g.nLT; ++p) {
+    const trax_layer_triplet& t = c->lts[p];
+    if (t.layer1 < 1 || t.layer2 < 1 || t.layer3 < 1 || t.layer1 > c->L || t.layer2 > c->L || t.layer3 > c->L)
+      return fail(c, TRAX_ERR_ARG, "layer triplet refers to a layer outside the uploaded layers");
+    g.layer1[p] = t.layer1;
+    g.layer2[p] = t.layer2;
+    g.layer3[p] = t.layer3;
+    g.dThetaCut[p] = t.dtheta_cut;
+    g.sigmaZ[p] = t.sigma_z;
+    g.dPhiCut[p] = t.dphi_cut;
+    g.sigmaPhi[p] = t.sigma_phi;
+    g.tipCut[p] = t.tip_cut;
+    g.z0[p] = t.z0;
+    float sp;  // Q1: pairSpreadPhi (uint) bound to the float* sigmaPhi parameter
+    memcpy(&sp, &t.pair_spread_phi, 4);
+    g.pairSigmaPhi[p] = sp;
+  }
+  if (c->minR.size() < c->L) return fail(c, TRAX_ERR_ARG, "geometry has fewer layers than the hits");
+  for (uint32_t l = 0; l < c->L; ++l) {
+    g.minR[l] = c->minR[l];
+    g.maxR[l] = c->maxR[l];
+  }
+  return TRAX_OK;
+}
+
+// read all slots (error word, counters, totals) in one copy
+int read_slots(trax_ctx* c) {
+  CK(cudaMemcpyAsync(c->hSlots, c->slots.p, sizeof(uint32_t) * S_N, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int read_slot(trax_ctx* c, int k, uint64_t* out) {
+  CK(cudaMemcpyAsync(c->hSlots + k, slot(c, k), sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  *out = c->hSlots[k];
+  return TRAX_OK;
+}
+
+int error_from_bits(trax_ctx* c, uint32_t bits) {
+  if (bits & TRAX_EBIT_TIMEOUT) return fail(c, TRAX_ERR_TIMEOUT, "a bounded device wait ran out");
+  if (bits & TRAX_EBIT_CAPACITY) return fail(c, TRAX_ERR_CAPACITY, "a stage produced more items than its capacity");
+  if (bits & TRAX_EBIT_BOUNDS) return fail(c, TRAX_ERR_DEVICE_ASSERT, "a device-side bounds check fired");
+  return TRAX_OK;
+}
+
+int check_device_error(trax_ctx* c) {
+  RC(read_slots(c));
+  c->pairSent = c->hSlots[S_PAIR_SENT];
+  c->candSent = c->hSlots[S_CAND_SENT];
+  return error_from_bits(c, c->hSlots[S_ERR]);
+}
+
+// Buffer holding n elements of sz bytes: allocated in SYNCED mode, checked in DEVICE mode.
+#define ENSURE(buf, n, sz)                                                      \
+  do {                                                                          \
+    if (mode == SYNCED) CK(ensure(c, c->buf, (size_t)(n) * (sz)));              \
+    else if ((size_t)(n) * (sz) > c->buf.cap)                                   \
+      return fail(c, TRAX_ERR_STATE, "device-mode buffer " #buf " too small");  \
+  } while (0)
+
+// exclusive scan of (count + 1) elements in place, count = nHost or *nDev;
+// the total is published into slot `dst` (clamped to cap)
+int scan_publish(trax_ctx* c, Mode mode, uint32_t* data, uint64_t nHost, const uint32_t* nDev, uint64_t maxCount,
+                 int dst, uint64_t cap) {
+  const uint64_t maxN = maxCount + 1;
+  if (mode == SYNCED) CK(ensure(c, c->scanScratch, scan_scratch_bytes(maxN)));
+  else if (scan_scratch_bytes(maxN) > c->scanScratch.cap)
+    return fail(c, TRAX_ERR_STATE, "device-mode scan scratch too small");
+  CK(scan_exclusive(data, data, nHost + 1, nDev, 1, maxN, c->scanScratch.p, dev_err(c), c->st, &c->launches));
+  CK(publish_total(data, nDev, nHost, cap, slot(c, dst), dev_err(c), c->st, &c->launches));
+  return TRAX_OK;
+}
+
+// ------------------------------------------------------------------ stages
+int stage_grid(trax_ctx* c, Mode mode) {
+  const uint64_t n = c->nHits;
+  const uint64_t cells = (uint64_t)c->E * c->L * c->cfg.C;
+  ENSURE(grid, cells, 4);
+  ENSURE(px, n, 4); ENSURE(py, n, 4); ENSURE(pz, n, 4);
+  ENSURE(player, n, 4); ENSURE(pdet, n, 4); ENSURE(phid, n, 4); ENSURE(pevt, n, 4); ENSURE(porig, n, 4);
+  ENSURE(pxyzp, n, 16);
+  ENSURE(sc_cell, n, 4); ENSURE(sc_phi, n, 4); ENSURE(sc_perm, n, 4);
+  if (c->cfg.C > 24576) ENSURE(sc_counts, cells, 4);
+  GridInput in;
+  in.x = ptr<float>(c->in_x);
+  in.y = ptr<float>(c->in_y);
+  in.z = ptr<float>(c->in_z);
+  in.layer = ptr<uint32_t>(c->in_layer);
+  in.det = ptr<uint32_t>(c->in_det);
+  in.hid = ptr<uint32_t>(c->in_hid);
+  in.evt = ptr<uint32_t>(c->in_evt);
+  in.eventOffsets = ptr<uint32_t>(c->evOff);
+  in.layerHits = ptr<uint32_t>(c->layHits);
+  in.layerOffsets = ptr<uint32_t>(c->layOff);
+  GridScratch sc;
+  sc.cell = ptr<uint32_t>(c->sc_cell);
+  sc.phi = ptr<float>(c->sc_phi);
+  sc.perm = ptr<uint32_t>(c->sc_perm);
+  sc.counts = ptr<uint32_t>(c->sc_counts);
+  CK(grid_build(c->cfg, in, ptr<uint32_t>(c->grid), dev_hits(c), sc, dev_err(c), c->st, &c->launches));
+  return TRAX_OK;
+}
+
+int stage_pairs(trax_ctx* c, Mode mode) {
+  const uint32_t S = c->cfg.E * c->cfg.nLT;
+  ENSURE(segOuter, S + 1, 4);
+  ENSURE(taskBase, S + 1, 4);
+  ENSURE(pairOffsets, S + 1, 4);
+  uint32_t* taskBase = ptr<uint32_t>(c->taskBase);
+  CK(pair_segments(c->cfg, ptr<uint32_t>(c->grid), ptr<uint32_t>(c->segOuter), taskBase, c->st, &c->launches));
+  RC(scan_publish(c, mode, taskBase, S, nullptr, S, S_TASKS, mode == DEVICE ? c->capTasks : NO_CAP));
+  const uint32_t* nTasksDev = slot(c, S_TASKS);
+  uint64_t maxTasks = c->capTasks;
+  if (mode == SYNCED) {
+    RC(read_slot(c, S_TASKS, &c->nTasks));
+    maxTasks = c->nTasks;
+  }
+  ENSURE(taskCount, maxTasks + 1, 4);
+  uint32_t* taskCount = ptr<uint32_t>(c->taskCount);
+  CK(pair_tasks(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
+                maxTasks, taskCount, nullptr, 0, slot(c, S_PAIR_SENT), dev_err(c), c->st, &c->launches));
+  RC(scan_publish(c, mode, taskCount, c->nTasks, mode == DEVICE ? nTasksDev : nullptr, maxTasks, S_PAIRS,
+                  mode == DEVICE ? c->capPairs : NO_CAP));
+  uint64_t maxPairs = c->capPairs;
+  if (mode == SYNCED) {
+    RC(read_slot(c, S_PAIRS, &c->nPairs));
+    maxPairs = c->nPairs;
+  }
+  ENSURE(pairs, maxPairs, 8);
+  CK(pair_tasks(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
+                maxTasks, taskCount, ptr<uint2>(c->pairs), maxPairs, slot(c, S_PAIR_SENT), dev_err(c), c->st,
+                &c->launches));
+  CK(pair_offsets(c->cfg, taskBase, taskCount, ptr<uint32_t>(c->pairOffsets), c->st, &c->launches));
+  return TRAX_OK;
+}
+
+int stage_predict(trax_ctx* c, Mode mode) {
+  const uint32_t S = c->cfg.E * c->cfg.nLT;
+  const uint32_t* nPairsDev = slot(c, S_PAIRS);
+  const uint64_t maxPairs = mode == SYNCED ? c->nPairs : c->capPairs;
+  ENSURE(candCount, maxPairs + 1, 4);
+  ENSURE(candOffsets, S + 1, 4);
+  uint32_t* candCount = ptr<uint32_t>(c->candCount);
+  CK(predict_pairs(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
+                   candCount, nullptr, 0, slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+  RC(scan_publish(c, mode, candCount, c->nPairs, mode == DEVICE ? nPairsDev : nullptr, maxPairs, S_CANDS,
+                  mode == DEVICE ? c->capCands : NO_CAP));
+  uint64_t maxCands = c->capCands;
+  if (mode == SYNCED) {
+    RC(read_slot(c, S_CANDS, &c->nCands));
+    maxCands = c->nCands;
+  }
+  ENSURE(cands, maxCands, 8);
+  CK(predict_pairs(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
+                   candCount, ptr<uint2>(c->cands), maxCands, slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+  CK(predict_offsets(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs, candCount,
+                     ptr<uint32_t>(c->candOffsets), c->st, &c->launches));
+  return TRAX_OK;
+}
+
+int stage_filter(trax_ctx* c, Mode mode) {
+  const uint32_t S = c->cfg.E * c->cfg.nLT;
+  const uint32_t* nCandsDev = slot(c, S_CANDS);
+  const uint64_t maxCands = mode == SYNCED ? c->nCands : c->capCands;
+  ENSURE(flags, maxCands + 1, 4);
+  ENSURE(tripOffsets, S + 1, 4);
+  uint32_t* flags = ptr<uint32_t>(c->flags);
+  CK(filter_candidates(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, flags,
+                       c->st, &c->launches));
+  RC(scan_publish(c, mode, flags, c->nCands, mode == DEVICE ? nCandsDev : nullptr, maxCands, S_TRIPLETS,
+                  mode == DEVICE ? c->capT : NO_CAP));
+  uint64_t maxT = c->capT;
+  if (mode == SYNCED) {
+    RC(read_slot(c, S_TRIPLETS, &c->nT));
+    maxT = c->nT;
+  }
+  ENSURE(h1, maxT, 4);
+  ENSURE(h2, maxT, 4);
+  ENSURE(h3, maxT, 4);
+  CK(filter_store(ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, flags, ptr<uint32_t>(c->h1),
+                  ptr<uint32_t>(c->h2), ptr<uint32_t>(c->h3), maxT, c->st, &c->launches));
+  CK(triplet_offsets(c->cfg, dev_hits(c), ptr<uint32_t>(c->h1), slot(c, S_TRIPLETS), maxT,
+                     ptr<uint32_t>(c->tripOffsets), c->st, &c->launches));
+  return TRAX_OK;
+}
+
+TripletView triplets(trax_ctx* c, uint64_t maxT) {
+  TripletView t;
+  t.h1 = ptr<uint32_t>(c->h1);
+  t.h2 = ptr<uint32_t>(c->h2);
+  t.h3 = ptr<uint32_t>(c->h3);
+  t.nDev = slot(c, S_TRIPLETS);
+  t.maxN = maxT;
+  return t;
+}
+
+int stage_connectivity(trax_ctx* c, Mode mode) {
+  const uint32_t S = c->cfg.E * c->cfg.nLT;
+  const uint64_t maxT = mode == SYNCED ? c->nT : c->capT;
+  const uint32_t* nTDev = slot(c, S_TRIPLETS);
+  if (mode == SYNCED) {
+    c->nLinks = c->nConn = c->nNonConn = c->nTracks = 0;
+    c->noLinks = true;
+  }
+  ENSURE(eta, maxT, 4);
+  ENSURE(segOf, maxT, 4);
+  ENSURE(segStart, S + 1, 4);
+  ENSURE(linkCount, maxT + 1, 4);
+  ENSURE(cflags, maxT + 1, 4);
+  ENSURE(connS, maxT + 1, 4);
+  ENSURE(nonConnS, maxT + 1, 4);
+  ENSURE(connIdx, maxT, 4);
+  ENSURE(nonConnIdx, maxT, 4);
+  TripletView tv = triplets(c, maxT);
+  CK(cudaMemsetAsync(c->cflags.p, 0, (size_t)(maxT + 1) * 4, c->st));
+  CK(triplet_eta(c->cfg, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->segOf), c->st, &c->launches));
+  CK(segment_bounds(c->cfg, ptr<uint32_t>(c->segOf), nTDev, ptr<uint32_t>(c->segStart), c->st, &c->launches));
+  uint32_t* linkCount = ptr<uint32_t>(c->linkCount);
+  CK(connectivity_tasks(c->cfg, false, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
+                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), nullptr, nullptr, 0, c->st,
+                        &c->launches));
+  RC(scan_publish(c, mode, linkCount, c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_LINKS,
+                  mode == DEVICE ? c->capLinks : NO_CAP));
+  uint64_t maxLinks = c->capLinks;
+  if (mode == SYNCED) {
+    RC(read_slot(c, S_LINKS, &c->nLinks));
+    maxLinks = c->nLinks;
+    c->noLinks = c->nLinks == 0;
+    if (c->noLinks) return TRAX_OK;  // TripletConnectivityTight.cpp:127-129
+  }
+  ENSURE(basis, maxLinks, 4);
+  ENSURE(follower, maxLinks, 4);
+  CK(connectivity_tasks(c->cfg, true, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
+                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), ptr<uint32_t>(c->basis),
+                        ptr<uint32_t>(c->follower), maxLinks, c->st, &c->launches));
+  CK(connectable_streams(ptr<uint32_t>(c->cflags), nTDev, maxT, ptr<uint32_t>(c->connS), ptr<uint32_t>(c->nonConnS),
+                         c->st, &c->launches));
+  RC(scan_publish(c, mode, ptr<uint32_t>(c->connS), c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_CONN, NO_CAP));
+  RC(scan_publish(c, mode, ptr<uint32_t>(c->nonConnS), c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_NONCONN,
+                  NO_CAP));
+  CK(compact_indices(ptr<uint32_t>(c->connS), nTDev, maxT, ptr<uint32_t>(c->connIdx), maxT, c->st, &c->launches));
+  CK(compact_indices(ptr<uint32_t>(c->nonConnS), nTDev, maxT, ptr<uint32_t>(c->nonConnIdx), maxT, c->st,
+                     &c->launches));
+  if (mode == SYNCED) {
+    RC(read_slots(c));
+    c->nConn = c->hSlots[S_CONN];
+    c->nNonConn = c->hSlots[S_NONCONN];
+  }
+  return TRAX_OK;
+}
+
+int stage_fit(trax_ctx* c, Mode mode) {
+  const uint64_t maxT = mode == SYNCED ? c->nT : c->capT;
+  ENSURE(pt, maxT, 4);
+  CK(cudaMemsetAsync(c->pt.p, 0, (size_t)std::max<uint64_t>(maxT, 1) * 4, c->st));
+  if (mode == SYNCED && c->noLinks) return TRAX_OK;
+  CK(circle_fit(dev_hits(c), triplets(c, maxT), ptr<uint32_t>(c->connIdx), slot(c, S_CONN), maxT, ptr<float>(c->pt),
+                c->st, &c->launches));
+  return TRAX_OK;
+}
+
+CABuffers ca_buffers(trax_ctx* c) {
+  CABuffers b;
+  b.states = ptr<uint32_t>(c->states);
+  b.inStart = ptr<uint32_t>(c->inStart);
+  b.inCursor = ptr<uint32_t>(c->inCursor);
+  b.inList = ptr<uint32_t>(c->inList);
+  b.best = ptr<uint32_t>(c->best);
+  b.isBest = ptr<uint32_t>(c->isBest);
+  b.handlers = ptr<uint32_t>(c->handlers);
+  b.segOf = ptr<uint32_t>(c->segOf);
+  return b;
+}
+
+int stage_ca(trax_ctx* c, Mode mode) {
+  if (mode == SYNCED && c->noLinks) {
+    c->nTracks = 0;
+    return TRAX_OK;
+  }
+  const uint64_t maxT = mode == SYNCED ? c->nT : c->capT;
+  const uint64_t maxLinks = mode == SYNCED ? c->nLinks : c->capLinks;
+  const uint32_t* nTDev = slot(c, S_TRIPLETS);
+  const uint32_t* nLinksDev = slot(c, S_LINKS);
+  ENSURE(states, maxT, 4);
+  ENSURE(inStart, maxT + 1, 4);
+  ENSURE(inCursor, maxT, 4);
+  ENSURE(inList, maxLinks, 4);
+  ENSURE(best, maxT, 4);
+  ENSURE(isBest, maxT, 4);
+  ENSURE(handlers, maxT + 1, 4);
+  CABuffers b = ca_buffers(c);
+  CK(ca_in_degree(ptr<uint32_t>(c->follower), nLinksDev, maxLinks, b, nTDev, maxT, c->st, &c->launches));
+  // in-degree prefix (its total is the number of links; not published)
+  if (mode == SYNCED) CK(ensure(c, c->scanScratch, scan_scratch_bytes(maxT + 1)));
+  CK(scan_exclusive(b.inStart, b.inStart, c->nT + 1, mode == DEVICE ? nTDev : nullptr, 1, maxT + 1,
+                    c->scanScratch.p, dev_err(c), c->st, &c->launches));
+  CK(ca_fill(ptr<uint32_t>(c->follower), nLinksDev, maxLinks, b, nTDev, maxT, c->st, &c->launches));
+  CK(ca_forward(c->cfg, ptr<uint32_t>(c->basis), b, nTDev, maxT, c->st, &c->launches));
+  CK(ca_backward(ptr<uint32_t>(c->basis), ptr<float>(c->pt), b, nTDev, maxT, nLinksDev, c->st, &c->launches));
+  RC(scan_publish(c, mode, b.handlers, c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_TRACKS,
+                  mode == DEVICE ? c->capTracks : NO_CAP));
+  uint64_t maxTracks = c->capTracks;
+  if (mode == SYNCED) {
+    RC(read_slot(c, S_TRACKS, &c->nTracks));
+    maxTracks = c->nTracks;
+  }
+  ENSURE(tracks, maxTracks, 4);
+  CK(ca_tracks(b, nTDev, maxT, ptr<uint32_t>(c->tracks), maxTracks, dev_err(c), c->st, &c->launches));
+  return TRAX_OK;
+}
+
+int begin_run(trax_ctx* c) {
+  RC(build_config(c));
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemsetAsync(c->slots.p, 0, sizeof(uint32_t) * S_N, c->st));
+  return TRAX_OK;
+}
+
+int run_stage(trax_ctx* c, int stage) {
+  if (stage > 1 && c->stage < stage - 1) return fail(c, TRAX_ERR_STATE, "the previous stage has not run");
+  int rc = TRAX_OK;
+  switch (stage) {
+    case 1: rc = begin_run(c); if (!rc) rc = stage_grid(c, SYNCED); break;
+    case 2: rc = stage_pairs(c, SYNCED); break;
+    case 3: rc = stage_predict(c, SYNCED); break;
+    case 4: rc = stage_filter(c, SYNCED); break;
+    case 5: rc = stage_connectivity(c, SYNCED); break;
+    case 6: rc = stage_fit(c, SYNCED); break;
+    case 7: rc = stage_ca(c, SYNCED); break;
+    default: return fail(c, TRAX_ERR_ARG, "unknown stage");
+  }
+  if (rc) return rc;
+  RC(check_device_error(c));
+  c->stage = stage;
+  return TRAX_OK;
+}
+
+int chain_device(trax_ctx* c, bool linking) {
+  RC(stage_grid(c, DEVICE));
+  RC(stage_pairs(c, DEVICE));
+  RC(stage_predict(c, DEVICE));
+  RC(stage_filter(c, DEVICE));
+  if (linking) {
+    RC(stage_connectivity(c, DEVICE));
+    RC(stage_fit(c, DEVICE));
+    RC(stage_ca(c, DEVICE));
+  }
+  return TRAX_OK;
+}
+
+uint64_t with_headroom(uint64_t n) { return n + n / 4 + 4096; }
+
+// Size every buffer for DEVICE mode from the sizes of the last SYNCED run.
+int size_device_buffers(trax_ctx* c) {
+  const Mode mode = SYNCED;
+  c->capTasks = with_headroom(c->nTasks);
+  c->capPairs = with_headroom(c->nPairs);
+  c->capCands = with_headroom(c->nCands);
+  c->capT = with_headroom(c->nT);
+  c->capLinks = with_headroom(c->nLinks);
+  c->capTracks = with_headroom(c->nTracks);
+  const uint32_t S = c->cfg.E * c->cfg.nLT;
+  ENSURE(taskCount, c->capTasks + 1, 4);
+  ENSURE(pairs, c->capPairs, 8);
+  ENSURE(candCount, c->capPairs + 1, 4);
+  ENSURE(cands, c->capCands, 8);
+  ENSURE(flags, c->capCands + 1, 4);
+  ENSURE(h1, c->capT, 4); ENSURE(h2, c->capT, 4); ENSURE(h3, c->capT, 4);
+  ENSURE(eta, c->capT, 4); ENSURE(segOf, c->capT, 4); ENSURE(segStart, S + 1, 4);
+  ENSURE(linkCount, c->capT + 1, 4); ENSURE(cflags, c->capT + 1, 4);
+  ENSURE(connS, c->capT + 1, 4); ENSURE(nonConnS, c->capT + 1, 4);
+  ENSURE(connIdx, c->capT, 4); ENSURE(nonConnIdx, c->capT, 4); ENSURE(pt, c->capT, 4);
+  ENSURE(basis, c->capLinks, 4); ENSURE(follower, c->capLinks, 4);
+  ENSURE(states, c->capT, 4); ENSURE(inStart, c->capT + 1, 4); ENSURE(inCursor, c->capT, 4);
+  ENSURE(inList, c->capLinks, 4); ENSURE(best, c->capT, 4); ENSURE(isBest, c->capT, 4);
+  ENSURE(handlers, c->capT + 1, 4); ENSURE(tracks, c->capTracks, 4);
+  uint64_t maxScan = std::max({c->capTasks, c->capPairs, c->capCands, c->capT, (uint64_t)S}) + 1;
+  CK(ensure(c, c->scanScratch, scan_scratch_bytes(maxScan)));
+  return TRAX_OK;
+}
+
+void drop_graph(trax_ctx* c) {
+  if (c->graphExec) cudaGraphExecDestroy(c->graphExec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graphExec = nullptr;
+  c->graph = nullptr;
+  c->graphKey = 0;
+}
+
+uint64_t shape_key(trax_ctx* c, bool linking) {
+  uint64_t k = 1469598103934665603ull;
+  auto mix = [&k](uint64_t v) {
+    k ^= v;
+    k *= 1099511628211ull;
+  };
+  mix(c->E); mix(c->L); mix(c->nHits); mix(c->cfg.C); mix(c->cfg.nLT); mix(linking ? 1 : 0);
+  mix(c->bufGeneration); mix(c->capTasks); mix(c->capPairs); mix(c->capCands); mix(c->capT); mix(c->capLinks);
+  mix(c->capTracks);
+  const unsigned char* b = reinterpret_cast<const unsigned char*>(&c->cfg);
+  for (size_t i = 0; i < sizeof(DevConfig); ++i) mix(b[i]);
+  return k;
+}
+
+int run_synced_chain(trax_ctx* c, bool linking) {
+  for (int s = 1; s <= (linking ? 7 : 4); ++s) RC(run_stage(c, s));
+  return TRAX_OK;
+}
+
+void fill_stats(trax_ctx* c, trax_batch_stats* s) {
+  if (!s) return;
+  memset(s, 0, sizeof(*s));
+  s->n_hits = c->nHits;
+  s->n_pairs = c->nPairs;
+  s->n_candidates = c->nCands;
+  s->n_triplets = c->nT;
+  s->n_links = c->nLinks;
+  s->n_connectable = c->nConn;
+  s->n_non_connectable = c->nNonConn;
+  s->n_track_entries = c->nTracks;
+  s->n_pair_sentinels = c->pairSent;
+  s->n_candidate_sentinels = c->candSent;
+  s->kernel_launches = c->launches;
+  s->device_ms = c->lastMs;
+}
+
+int copy_out(trax_ctx* c, void* dst, const DevBuf& src, size_t bytes) {
+  if (!dst || bytes == 0) return TRAX_OK;
+  CK(cudaMemcpyAsync(dst, src.p, bytes, cudaMemcpyDeviceToHost, c->st));
+  return TRAX_OK;
+}
+
+}  // namespace
+
+// ======================================================================= C ABI
+extern "C" {
+
+const char* trax_version(void) { return kVersion; }
+
+int trax_create(trax_ctx** out, int device) {
+  if (!out) return TRAX_ERR_ARG;
+  *out = nullptr;
+  trax_ctx* c = new trax_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->hSlots, sizeof(uint32_t) * 64);
+  if (e == cudaSuccess) e = ensure(c, c->slots, sizeof(uint32_t) * 64);
+  if (e == cudaSuccess) e = cudaMemset(c->slots.p, 0, sizeof(uint32_t) * 64);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = grid_prepare(device);
+  if (e != cudaSuccess) {
+    trax_destroy(c);
+    return TRAX_ERR_CUDA;
+  }
+  *out = c;
+  return TRAX_OK;
+}
+
+void trax_destroy(trax_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  drop_graph(c);
+  DevBuf* bufs[] = {&c->in_x, &c->in_y, &c->in_z, &c->in_layer, &c->in_det, &c->in_hid, &c->in_evt, &c->evOff,
+                    &c->layHits, &c->layOff, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
+                    &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
+                    &c->segOuter, &c->taskBase, &c->taskCount, &c->pairs, &c->pairOffsets, &c->candCount, &c->cands,
+                    &c->candOffsets, &c->flags, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
+                    &c->segStart, &c->linkCount, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS,
+                    &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,
+                    &c->isBest, &c->handlers, &c->tracks, &c->scanScratch, &c->slots};
+  for (DevBuf* b : bufs) release(*b);
+  if (c->hSlots) cudaFreeHost(c->hSlots);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+}
+
+const char* trax_last_error(const trax_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int trax_set_layer_triplets(trax_ctx* c, const trax_layer_triplet* lt, int n, float min_pt) {
+  if (!c || !lt || n <= 0) return fail(c, TRAX_ERR_ARG, "need at least one layer triplet");
+  if (n > TRAX_MAX_LT) return fail(c, TRAX_ERR_ARG, "too many layer triplets");
+  for (int p = 0; p < n; ++p) {
+    if (lt[p].layer1 != (uint32_t)p + 1)
+      return fail(c, TRAX_ERR_ARG, "layer triplet p must start on layer p+1 (the layer-triplet index is derived "
+                                   "from the first hit's layer)");
+    if (lt[p].layer2 <= lt[p].layer1 || lt[p].layer3 <= lt[p].layer2)
+      return fail(c, TRAX_ERR_ARG, "layer triplets must run outwards (layer1 < layer2 < layer3)");
+  }
+  c->lts.assign(lt, lt + n);
+  c->minPt = min_pt;
+  c->haveLT = true;
+  c->stage = 0;
+  return TRAX_OK;
+}
+
+int trax_set_geometry(trax_ctx* c, const float* min_r, const float* max_r, int n_layers) {
+  if (!c || !min_r || !max_r || n_layers <= 0 || n_layers > TRAX_MAX_LAYERS)
+    return fail(c, TRAX_ERR_ARG, "invalid geometry");
+  c->minR.assign(min_r, min_r + n_layers);
+  c->maxR.assign(max_r, max_r + n_layers);
+  c->haveGeom = true;
+  c->stage = 0;
+  return TRAX_OK;
+}
+
+int trax_set_grid(trax_ctx* c, uint32_t n_z, uint32_t n_phi) {
+  if (!c || n_z == 0 || n_phi == 0) return fail(c, TRAX_ERR_ARG, "grid needs at least one z and one phi sector");
+  if ((uint64_t)(n_z + 1) * (n_phi + 1) > (1u << 22)) return fail(c, TRAX_ERR_ARG, "grid too large");
+  c->nZ = n_z;
+  c->nP = n_phi;
+  c->haveGrid = true;
+  c->stage = 0;
+  return TRAX_OK;
+}
+
+int trax_upload_hits(trax_ctx* c, const trax_hits_soa* h, uint32_t n_hits, const uint32_t* event_offsets,
+                     const uint32_t* layer_hits, const uint32_t* layer_offsets, uint32_t n_events,
+                     uint32_t n_layers) {
+  if (!c || !h || !event_offsets || !layer_hits || !layer_offsets) return fail(c, TRAX_ERR_ARG, "null argument");
+  if (n_layers == 0 || n_layers > TRAX_MAX_LAYERS) return fail(c, TRAX_ERR_ARG, "invalid number of layers");
+  // the supplements must describe the hits contiguously (HitCollection.cpp:120-133)
+  uint64_t pos = 0;
+  for (uint32_t e = 0; e < n_events; ++e) {
+    if (event_offsets[e] != pos) return fail(c, TRAX_ERR_ARG, "event offsets are not contiguous");
+    uint64_t lpos = 0;
+    for (uint32_t l = 0; l < n_layers; ++l) {
+      const size_t k = (size_t)e * n_layers + l;
+      if (layer_offsets[k] != lpos) return fail(c, TRAX_ERR_ARG, "layer offsets are not contiguous");
+      lpos += layer_hits[k];
+    }
+    pos += lpos;
+  }
+  if (pos != n_hits) return fail(c, TRAX_ERR_ARG, "supplements do not add up to n_hits");
+  const Mode mode = SYNCED;
+  const size_t n = n_hits;
+  ENSURE(in_x, n, 4); ENSURE(in_y, n, 4); ENSURE(in_z, n, 4);
+  ENSURE(in_layer, n, 4); ENSURE(in_det, n, 4); ENSURE(in_hid, n, 4); ENSURE(in_evt, n, 4);
+  ENSURE(evOff, n_events, 4);
+  ENSURE(layHits, (size_t)n_events * n_layers, 4);
+  ENSURE(layOff, (size_t)n_events * n_layers, 4);
+  CK(cudaMemcpyAsync(c->in_x.p, h->x, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->in_y.p, h->y, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->in_z.p, h->z, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->in_layer.p, h->layer, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->in_det.p, h->det_id, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->in_hid.p, h->hit_id, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->in_evt.p, h->event, n * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->evOff.p, event_offsets, (size_t)n_events * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->layHits.p, layer_hits, (size_t)n_events * n_layers * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->layOff.p, layer_offsets, (size_t)n_events * n_layers * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->E = n_events;
+  c->L = n_layers;
+  c->nHits = n_hits;
+  c->haveHits = true;
+  c->stage = 0;
+  return TRAX_OK;
+}
+
+int trax_grid_build(trax_ctx* c) { return c ? run_stage(c, 1) : TRAX_ERR_ARG; }
+
+int trax_pair_gen(trax_ctx* c, uint64_t* n_pairs) {
+  if (!c) return TRAX_ERR_ARG;
+  RC(run_stage(c, 2));
+  if (n_pairs) *n_pairs = c->nPairs;
+  return TRAX_OK;
+}
+
+int trax_triplet_predict(trax_ctx* c, uint64_t* n_candidates) {
+  if (!c) return TRAX_ERR_ARG;
+  RC(run_stage(c, 3));
+  if (n_candidates) *n_candidates = c->nCands;
+  return TRAX_OK;
+}
+
+int trax_triplet_filter(trax_ctx* c, uint64_t* n_triplets) {
+  if (!c) return TRAX_ERR_ARG;
+  RC(run_stage(c, 4));
+  if (n_triplets) *n_triplets = c->nT;
+  return TRAX_OK;
+}
+
+int trax_connectivity(trax_ctx* c, float d_eta_cut, uint64_t* n_links) {
+  if (!c) return TRAX_ERR_ARG;
+  c->dEtaCut = d_eta_cut;
+  c->cfg.dEtaCut = d_eta_cut;
+  RC(run_stage(c, 5));
+  if (n_links) *n_links = c->nLinks;
+  return TRAX_OK;
+}
+
+int trax_circle_fit(trax_ctx* c) { return c ? run_stage(c, 6) : TRAX_ERR_ARG; }
+
+int trax_cellular_automaton(trax_ctx* c, uint64_t* n_track_entries) {
+  if (!c) return TRAX_ERR_ARG;
+  RC(run_stage(c, 7));
+  if (n_track_entries) *n_track_entries = c->nTracks;
+  return TRAX_OK;
+}
+
+int trax_prefix_sum(trax_ctx* c, uint32_t* data, uint64_t n) {
+  if (!c || (!data && n)) return fail(c, TRAX_ERR_ARG, "null data");
+  if (n == 0) return TRAX_OK;
+  if (n > 0xffffffffull) return fail(c, TRAX_ERR_ARG, "scan length above 2^32 - 1");
+  DevBuf tmp;
+  CK(ensure(c, tmp, n * 4));
+  int rc = TRAX_OK;
+  cudaError_t e = cudaMemcpyAsync(tmp.p, data, n * 4, cudaMemcpyHostToDevice, c->st);
+  if (e == cudaSuccess) e = ensure(c, c->scanScratch, scan_scratch_bytes(n));
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->slots.p, 0, 4, c->st);
+  if (e == cudaSuccess)
+    e = scan_exclusive(ptr<uint32_t>(tmp), ptr<uint32_t>(tmp), n, nullptr, 0, n, c->scanScratch.p, dev_err(c), c->st,
+                       &c->launches);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(data, tmp.p, n * 4, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) rc = cuda_fail(c, e, "trax_prefix_sum");
+  release(tmp);
+  if (rc == TRAX_OK) rc = check_device_error(c);
+  return rc;
+}
+
+int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* stats) {
+  if (!c) return TRAX_ERR_ARG;
+  const bool linking = opts ? opts->run_linking != 0 : true;
+  const bool useGraph = opts ? opts->use_graph != 0 : false;
+  if (opts && opts->d_eta_cut > 0.0f) c->dEtaCut = opts->d_eta_cut;
+  c->launches = 0;
+  if (!useGraph) {
+    CK(cudaEventRecord(c->ev0, c->st));
+    RC(run_synced_chain(c, linking));
+    CK(cudaEventRecord(c->ev1, c->st));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->lastMs = ms;
+    fill_stats(c, stats);
+    return TRAX_OK;
+  }
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    RC(build_config(c));
+    const uint64_t key = shape_key(c, linking);
+    if (!c->graphExec || key != c->graphKey) {
+      // calibrate the capacities with one host-synced run, then capture
+      drop_graph(c);
+      RC(run_synced_chain(c, linking));
+      RC(size_device_buffers(c));
+      c->launches = 0;
+      CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+      cudaMemsetAsync(c->slots.p, 0, sizeof(uint32_t) * S_N, c->st);
+      int rc = chain_device(c, linking);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(c->st, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+      c->graph = g;
+      CK(cudaGraphInstantiate(&c->graphExec, g, 0));
+      c->graphLaunches = c->launches;
+      c->graphKey = shape_key(c, linking);
+    }
+    CK(cudaEventRecord(c->ev0, c->st));
+    CK(cudaGraphLaunch(c->graphExec, c->st));
+    CK(cudaEventRecord(c->ev1, c->st));
+    RC(read_slots(c));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->lastMs = ms;
+    c->launches = c->graphLaunches;
+    const uint32_t bits = c->hSlots[S_ERR];
+    c->nTasks = c->hSlots[S_TASKS];
+    c->nPairs = c->hSlots[S_PAIRS];
+    c->nCands = c->hSlots[S_CANDS];
+    c->nT = c->hSlots[S_TRIPLETS];
+    c->nLinks = linking ? c->hSlots[S_LINKS] : 0;
+    c->nConn = linking ? c->hSlots[S_CONN] : 0;
+    c->nNonConn = linking ? c->hSlots[S_NONCONN] : 0;
+    c->nTracks = linking ? c->hSlots[S_TRACKS] : 0;
+    c->noLinks = c->nLinks == 0;
+    if (c->noLinks) c->nConn = c->nNonConn = c->nTracks = 0;  // the reference returns no lists then
+    c->pairSent = c->hSlots[S_PAIR_SENT];
+    c->candSent = c->hSlots[S_CAND_SENT];
+    if (bits & TRAX_EBIT_CAPACITY) {
+      // admission failed: recalibrate on these events and replay once more
+      drop_graph(c);
+      continue;
+    }
+    RC(error_from_bits(c, bits));
+    c->stage = linking ? 7 : 4;
+    fill_stats(c, stats);
+    return TRAX_OK;
+  }
+  return fail(c, TRAX_ERR_CAPACITY, "capacity exceeded after recalibration");
+}
+
+int trax_get_stats(trax_ctx* c, trax_batch_stats* s) {
+  if (!c || !s) return TRAX_ERR_ARG;
+  fill_stats(c, s);
+  return TRAX_OK;
+}
+
+int trax_get_pairs(trax_ctx* c, uint32_t* pairs2, uint32_t* offsets) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 2) return fail(c, TRAX_ERR_STATE, "pairs not generated");
+  RC(copy_out(c, pairs2, c->pairs, c->nPairs * 8));
+  RC(copy_out(c, offsets, c->pairOffsets, ((size_t)c->cfg.E * c->cfg.nLT + 1) * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_get_candidates(trax_ctx* c, uint32_t* cands2, uint32_t* offsets) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 3) return fail(c, TRAX_ERR_STATE, "candidates not predicted");
+  RC(copy_out(c, cands2, c->cands, c->nCands * 8));
+  RC(copy_out(c, offsets, c->candOffsets, ((size_t)c->cfg.E * c->cfg.nLT + 1) * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_get_triplets(trax_ctx* c, uint32_t* h1, uint32_t* h2, uint32_t* h3, uint32_t* offsets) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 4) return fail(c, TRAX_ERR_STATE, "triplets not filtered");
+  RC(copy_out(c, h1, c->h1, c->nT * 4));
+  RC(copy_out(c, h2, c->h2, c->nT * 4));
+  RC(copy_out(c, h3, c->h3, c->nT * 4));
+  RC(copy_out(c, offsets, c->tripOffsets, ((size_t)c->cfg.E * c->cfg.nLT + 1) * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_get_triplet_eta_pt(trax_ctx* c, float* eta, float* pt) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 5) return fail(c, TRAX_ERR_STATE, "connectivity not run");
+  RC(copy_out(c, eta, c->eta, c->nT * 4));
+  if (c->stage >= 6) RC(copy_out(c, pt, c->pt, c->nT * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_get_links(trax_ctx* c, uint32_t* basis, uint32_t* follower, uint32_t* connectable, uint32_t* non_connectable) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 5) return fail(c, TRAX_ERR_STATE, "connectivity not run");
+  if (c->noLinks) return TRAX_OK;
+  RC(copy_out(c, basis, c->basis, c->nLinks * 4));
+  RC(copy_out(c, follower, c->follower, c->nLinks * 4));
+  RC(copy_out(c, connectable, c->connIdx, c->nConn * 4));
+  RC(copy_out(c, non_connectable, c->nonConnIdx, c->nNonConn * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_get_tracks(trax_ctx* c, uint32_t* states, uint32_t* tracks, uint32_t* track_offsets) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage >= 5 && c->noLinks) return TRAX_OK;  // no links: the reference runs no CA
+  if (c->stage < 7) return fail(c, TRAX_ERR_STATE, "cellular automaton not run");
+  RC(copy_out(c, states, c->states, c->nT * 4));
+  RC(copy_out(c, tracks, c->tracks, c->nTracks * 4));
+  RC(copy_out(c, track_offsets, c->handlers, (c->nT + 1) * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_get_grid(trax_ctx* c, uint32_t* grid, uint64_t* n_cells) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 1) return fail(c, TRAX_ERR_STATE, "grid not built");
+  const uint64_t cells = (uint64_t)c->E * c->L * c->cfg.C;
+  if (n_cells) *n_cells = cells;
+  RC(copy_out(c, grid, c->grid, cells * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_get_hit_perm(trax_ctx* c, uint32_t* perm) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 1) return fail(c, TRAX_ERR_STATE, "grid not built");
+  RC(copy_out(c, perm, c->porig, (size_t)c->nHits * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+}  // extern "C"

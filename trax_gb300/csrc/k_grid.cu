@@ -1,0 +1,142 @@
+// k_grid.cu -- per-(event, layer) z/phi grid and grid-ordered hit collection.
+//
+// Replaces gridCount / PrefixSum / gridStore (GridBuilder.h:48-427,
+// GridBuilder.cpp:6-161).  One CTA owns one (event, layer): it histograms its
+// hits into shared-memory cell counters, scans them in the CTA (the offset of
+// the layer inside the event batch is known from the supplements, so the
+// global scan of the reference reduces to base + local scan), places every
+// hit at a STABLE slot (hits keep their input order inside a cell, one of
+// the orders the reference's atomic_inc can produce) and finally gathers the
+// seven hit columns into cell order with coalesced stores.  It also writes
+// the packed (x, y, z, phi) array the candidate loops read with one 16-byte
+// load, phi being the same atan2 the cell assignment used.
+#include "trax_kernels.h"
+
+namespace trax {
+
+namespace {
+
+constexpr int GRID_THREADS = 256;
+constexpr int GRID_WARPS = GRID_THREADS / 32;
+// cell counters live in shared memory up to this many cells
+constexpr uint32_t GRID_SMEM_CELLS = 24576;  // 96 KB
+
+__global__ void __launch_bounds__(GRID_THREADS)
+    grid_kernel(DevConfig cfg, GridInput in, uint32_t* __restrict__ grid, DevHits out, GridScratch sc,
+                uint32_t* err, int useSmem) {
+  extern __shared__ uint32_t smem[];
+  __shared__ uint32_t s_warpSum[GRID_WARPS];
+  const uint32_t task = blockIdx.x;  // event * L + layer
+  const uint32_t e = task / cfg.L;
+  const uint32_t C = cfg.C;
+  const uint32_t n = in.layerHits[task];
+  const uint32_t base = in.eventOffsets[e] + in.layerOffsets[task];
+  uint32_t* cnt = useSmem ? smem : sc.counts + (size_t)task * C;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+
+  for (uint32_t c = tid; c < C; c += GRID_THREADS) cnt[c] = 0u;
+  __syncthreads();
+
+  // 1. cells (gridCount, GridBuilder.h:80-87)
+  for (uint32_t i = tid; i < n; i += GRID_THREADS) {
+    const uint32_t k = base + i;
+    const float x = in.x[k], y = in.y[k], z = in.z[k];
+    uint32_t zSector = f2u_sat(floor_(div_(z - cfg.minZ, cfg.sZ)));
+    float phi = atan2_(y, x);
+    uint32_t phiSector = f2u_sat(floor_(div_(phi - cfg.minPhi, cfg.sP)));
+    if (zSector >= cfg.nZ || phiSector > cfg.nP) {
+      raise_error(err, TRAX_EBIT_BOUNDS);
+      zSector = min(zSector, cfg.nZ - 1);
+      phiSector = min(phiSector, cfg.nP);
+    }
+    const uint32_t cell = zSector * (cfg.nP + 1) + phiSector;
+    sc.cell[k] = cell;
+    sc.phi[k] = phi;
+    atomicAdd(&cnt[cell], 1u);
+  }
+  __syncthreads();
+
+  // 2. CTA exclusive scan of the counters; write the grid boundaries
+  const uint32_t chunk = (C + GRID_THREADS - 1) / GRID_THREADS;
+  const uint32_t c0 = min(tid * chunk, C), c1 = min(c0 + chunk, C);
+  uint32_t local = 0;
+  for (uint32_t c = c0; c < c1; ++c) local += cnt[c];
+  uint32_t incl = local;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += t;
+  }
+  if (lane == 31) s_warpSum[warp] = incl;
+  __syncthreads();
+  uint32_t warpOff = 0;
+  for (uint32_t w = 0; w < warp; ++w) warpOff += s_warpSum[w];
+  uint32_t run = warpOff + incl - local;
+  __syncthreads();
+  uint32_t* gl = grid + (size_t)task * C;
+  for (uint32_t c = c0; c < c1; ++c) {
+    uint32_t v = cnt[c];
+    cnt[c] = run;  // becomes the next free slot of the cell
+    gl[c] = base + run;
+    run += v;
+  }
+  __syncthreads();
+
+  // 3. stable placement: chunks of GRID_THREADS hits in input order, warps
+  //    of a chunk take their turn so that lower input indices get lower slots
+  for (uint32_t c0h = 0; c0h < n; c0h += GRID_THREADS) {
+    const uint32_t i = c0h + tid;
+    const bool valid = i < n;
+    const uint32_t cell = valid ? sc.cell[base + i] : 0xffffffffu;
+    for (uint32_t w = 0; w < GRID_WARPS; ++w) {
+      if (warp == w && c0h + w * 32 < n) {
+        const uint32_t peers = __match_any_sync(0xffffffffu, cell);
+        if (valid) {
+          const uint32_t leader = __ffs(peers) - 1;
+          const uint32_t rank = __popc(peers & lanemask_lt());
+          uint32_t slot0 = 0;
+          if (lane == leader) slot0 = atomicAdd(&cnt[cell], (uint32_t)__popc(peers));
+          slot0 = __shfl_sync(peers, slot0, leader);
+          sc.perm[base + slot0 + rank] = i;
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // 4. gather into cell order (gridStore, GridBuilder.h:243-253)
+  for (uint32_t s = tid; s < n; s += GRID_THREADS) {
+    const uint32_t dst = base + s;
+    const uint32_t src = base + sc.perm[dst];
+    const float x = in.x[src], y = in.y[src], z = in.z[src];
+    out.x[dst] = x;
+    out.y[dst] = y;
+    out.z[dst] = z;
+    out.layer[dst] = in.layer[src];
+    out.det[dst] = in.det[src];
+    out.hid[dst] = in.hid[src];
+    out.evt[dst] = in.evt[src];
+    out.orig[dst] = src;
+    out.xyzp[dst] = make_float4(x, y, z, sc.phi[src]);
+  }
+}
+
+}  // namespace
+
+cudaError_t grid_prepare(int) {
+  return cudaFuncSetAttribute(grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(GRID_SMEM_CELLS * sizeof(uint32_t)));
+}
+
+cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid, DevHits out, GridScratch sc,
+                       uint32_t* err, cudaStream_t st, uint32_t* launches) {
+  const uint32_t tasks = cfg.E * cfg.L;
+  if (tasks == 0) return cudaSuccess;
+  const int useSmem = cfg.C <= GRID_SMEM_CELLS ? 1 : 0;
+  const size_t smemBytes = useSmem ? (size_t)cfg.C * sizeof(uint32_t) : 0;
+  grid_kernel<<<tasks, GRID_THREADS, smemBytes, st>>>(cfg, in, grid, out, sc, err, useSmem);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace trax

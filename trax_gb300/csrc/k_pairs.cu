@@ -1,0 +1,290 @@
+// k_pairs.cu -- hit-pair generation from beamspot windows.
+//
+// Replaces pairCount / PrefixSum / pairStore (PairGeneratorBeamspot.h:43-525,
+// PairGeneratorBeamspot.cpp:5-183) without the reference's n1 x n2 bit
+// "oracle": the count pass counts, per outer hit, the valid visits of the
+// reference's cell loop (duplicates included -- that is the reference's
+// count), the exclusive scan turns counts into positions, and the store pass
+// re-runs the window and writes the DISTINCT valid inner hits in ascending
+// index order, which is the order pairStore's bitmap walk produces with one
+// work-item per outer hit.  Slots the reference never writes (count larger
+// than the distinct hits: windows wider than 2 pi) get the sentinel pair
+// (0xffffffff, 0xffffffff).
+//
+// The visit set of one z row is the reference's j loop
+//   for (j = grid[row + pL]; j < end2; ++j) index = j - (j >= zEnd) * len
+// rewritten as two index ranges, P1 = [J0, min(end2, zEnd)) and
+// P2 = [max(J0, zEnd) - len, end2 - len).  When all ranges of an outer hit
+// are disjoint and can be ordered, the store pass walks them in ascending
+// order; otherwise (only for NaN/inf or > 2 pi windows) it walks the whole
+// inner layer and keeps the indices that some range contains.
+#include "trax_kernels.h"
+
+namespace trax {
+
+namespace {
+
+constexpr int PAIR_THREADS = 128;
+
+struct PairWindow {
+  float zLow, zHigh, phiLow, phiHigh;
+  uint32_t zLowSector, zHighSector, pL, pH;
+  uint32_t wrap;
+};
+
+// The window arithmetic of pairCount (PairGeneratorBeamspot.h:111-162), in
+// the reference's operation order (Q1 sigmaPhi bit pattern, Q2 signed
+// radius, Q3 atan-then-divide, Q5 select-by-multiply).
+__device__ __forceinline__ PairWindow pair_window(const DevConfig& cfg, uint32_t p, float x, float y, float z,
+                                                  float phi) {
+  const uint32_t layer = cfg.layer1[p] - 1;
+  const float z0 = cfg.z0[p];
+  const float tip = cfg.tipCut[p];
+  const float sigmaZ = cfg.sigmaZ[p];
+  const float sigmaPhi = cfg.pairSigmaPhi[p];
+  const float minR1 = cfg.minR[layer];
+  const float maxR1 = cfg.maxR[layer];
+  PairWindow w;
+  float signRadius = cl_sign(y);
+  float r = signRadius * sqrt_(x * x + y * y);
+  float cotThetaHigh = div_(z - z0, r);
+  float cotThetaLow = div_(z + z0, r);
+  float tmp = signRadius * maxR1 * cotThetaHigh + z0;
+  float zHigh = signRadius * minR1 * cotThetaHigh + z0;
+  zHigh = (float)(tmp < zHigh) * zHigh + (float)(tmp > zHigh) * tmp;
+  tmp = signRadius * maxR1 * cotThetaLow - z0;
+  float zLow = signRadius * minR1 * cotThetaLow - z0;
+  zLow = (float)(tmp < zLow) * tmp + (float)(tmp > zLow) * zLow;
+  zLow -= sigmaZ;
+  zHigh += sigmaZ;
+  w.zLowSector = (uint32_t)max(f2i_sat(floor_(div_(zLow - cfg.minZ, cfg.sZ))), 0);
+  w.zHighSector = min(f2u_sat(floor_(div_(zHigh - cfg.minZ, cfg.sZ))) + 1u, cfg.nZ);
+  const float twoR = 2 * cfg.minRcurv;
+  tmp = fabs_(acos_(div_(r, twoR)) - acos_(div_(maxR1, twoR)));
+  float dPhi = fabs_(acos_(div_(r, twoR)) - acos_(div_(minR1, twoR)));
+  dPhi = (float)(tmp < dPhi) * dPhi + (float)(tmp > dPhi) * tmp;
+  tmp = div_(atan_(tip * (r - minR1)), r * minR1);
+  float phiHigh = div_(atan_(tip * (r - maxR1)), r * maxR1);
+  dPhi += tmp > phiHigh ? tmp : phiHigh;
+  float phiLow = phi - dPhi - sigmaPhi;
+  phiHigh = phi + dPhi + sigmaPhi;
+  const bool wrapAround = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
+  phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  w.pL = f2u_sat(floor_(div_(phiLow - cfg.minPhi, cfg.sP)));
+  w.pH = f2u_sat(floor_(div_(phiHigh - cfg.minPhi, cfg.sP)) + 1);
+  w.zLow = zLow;
+  w.zHigh = zHigh;
+  w.phiLow = phiLow;
+  w.phiHigh = phiHigh;
+  w.wrap = wrapAround ? 1u : 0u;
+  return w;
+}
+
+__device__ __forceinline__ bool pair_valid(const PairWindow& w, float4 h) {
+  bool valid = w.zLow <= h.z && h.z <= w.zHigh;
+  const float actPhi = h.w;
+  return valid && ((!w.wrap && (w.phiLow <= actPhi && actPhi <= w.phiHigh)) ||
+                   (w.wrap && ((w.phiLow <= actPhi && actPhi <= TRAX_PI_F) ||
+                               (-TRAX_PI_F <= actPhi && actPhi <= w.phiHigh))));
+}
+
+// visit ranges of one z row (pair generation: zEnd is the start of the phi
+// overflow column, PairGeneratorBeamspot.h:174-185)
+__device__ __forceinline__ void pair_row_parts(const PairWindow& w, const uint32_t* lG, uint32_t C, uint32_t nP,
+                                               uint32_t zs, uint32_t& a1, uint32_t& b1, uint32_t& a2,
+                                               uint32_t& b2) {
+  const uint32_t row = zs * (nP + 1);
+  const uint32_t zStart = cell_at(lG, row, C);
+  const uint32_t zEnd = cell_at(lG, row + nP, C);  // (zSector+1)*(nP+1)-1
+  const uint32_t len = zEnd - zStart;
+  const uint32_t J0 = cell_at(lG, row + w.pL, C);
+  const uint32_t end2 = w.wrap * zEnd + cell_at(lG, row + w.pH, C) - w.wrap * zStart;
+  a1 = J0;
+  b1 = min(end2, zEnd);
+  if (b1 < a1) b1 = a1;
+  const uint32_t j2 = max(J0, zEnd);
+  if (j2 < end2) {
+    a2 = j2 - len;
+    b2 = end2 - len;
+  } else {
+    a2 = b2 = 0;
+  }
+}
+
+__device__ __forceinline__ uint32_t find_segment(const uint32_t* taskBase, uint32_t S, uint32_t k) {
+  // largest s with taskBase[s] <= k
+  uint32_t lo = 0, hi = S;  // taskBase[S] > k
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (taskBase[mid] <= k) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void segments_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, uint32_t* segOuter,
+                                uint32_t* segCount) {
+  const uint32_t S = cfg.E * cfg.nLT;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+    const uint32_t e = s / cfg.nLT, p = s % cfg.nLT;
+    const uint32_t* lG2 = grid + ((size_t)e * cfg.L + (cfg.layer2[p] - 1)) * cfg.C;
+    const uint32_t l2off = lG2[0];
+    segOuter[s] = l2off;
+    segCount[s] = lG2[cfg.C - 1] - l2off;  // PairGeneratorBeamspot.h:70-73
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) segCount[S] = 0u;
+}
+
+template <bool EMIT>
+__global__ void __launch_bounds__(PAIR_THREADS)
+    pair_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
+                const uint32_t* __restrict__ segOuter, const uint32_t* __restrict__ taskBase,
+                const uint32_t* __restrict__ nTasksDev, uint32_t* taskCount, uint2* pairs, uint32_t capPairs,
+                uint32_t* sentinels, uint32_t* err) {
+  const uint32_t S = cfg.E * cfg.nLT;
+  const uint32_t nTasks = *nTasksDev;
+  const uint32_t C = cfg.C, nP = cfg.nP;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nTasks; k += gridDim.x * blockDim.x) {
+    const uint32_t s = find_segment(taskBase, S, k);
+    const uint32_t e = s / cfg.nLT, p = s % cfg.nLT;
+    const uint32_t i = segOuter[s] + (k - taskBase[s]);
+    const float4 ho = hits[i];
+    const PairWindow w = pair_window(cfg, p, ho.x, ho.y, ho.z, ho.w);
+    const uint32_t* lG1 = grid + ((size_t)e * cfg.L + (cfg.layer1[p] - 1)) * C;
+    if (!EMIT) {
+      uint32_t nFound = 0;
+      for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
+        uint32_t a1, b1, a2, b2;
+        pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
+        for (uint32_t j = a1; j < b1; ++j) nFound += pair_valid(w, hits[j]);
+        for (uint32_t j = a2; j < b2; ++j) nFound += pair_valid(w, hits[j]);
+      }
+      taskCount[k] = nFound;
+      if (k == 0) taskCount[nTasks] = 0u;
+    } else {
+      const uint32_t pos0 = taskCount[k];
+      uint32_t limit = taskCount[k + 1] - pos0;
+      if (pos0 >= capPairs) limit = 0;
+      else if (limit > capPairs - pos0) limit = capPairs - pos0;
+      uint2* out = pairs + pos0;
+      // ordering check: ranges disjoint and ascending
+      bool simple = true;
+      uint32_t prevEnd = 0;
+      for (uint32_t zs = w.zLowSector; zs < w.zHighSector && simple; ++zs) {
+        uint32_t a1, b1, a2, b2;
+        pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
+        const bool n1 = a1 < b1, n2 = a2 < b2;
+        if (n1 && n2) {
+          if (b2 <= a1) {
+            simple = a2 >= prevEnd;
+            prevEnd = b1;
+          } else if (b1 <= a2) {
+            simple = a1 >= prevEnd;
+            prevEnd = b2;
+          } else {
+            simple = false;
+          }
+        } else if (n1) {
+          simple = a1 >= prevEnd;
+          prevEnd = b1;
+        } else if (n2) {
+          simple = a2 >= prevEnd;
+          prevEnd = b2;
+        }
+      }
+      uint32_t written = 0;
+      if (simple) {
+        for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
+          uint32_t a1, b1, a2, b2;
+          pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
+          uint32_t lo0 = a1, hi0 = b1, lo1 = a2, hi1 = b2;
+          if (a2 < b2 && b2 <= a1) {  // P2 precedes P1
+            lo0 = a2; hi0 = b2; lo1 = a1; hi1 = b1;
+          }
+          for (uint32_t j = lo0; j < hi0; ++j)
+            if (pair_valid(w, hits[j])) {
+              if (written < limit) out[written] = make_uint2(j, i);
+              ++written;
+            }
+          for (uint32_t j = lo1; j < hi1; ++j)
+            if (pair_valid(w, hits[j])) {
+              if (written < limit) out[written] = make_uint2(j, i);
+              ++written;
+            }
+        }
+        if (written != limit) raise_error(err, TRAX_EBIT_BOUNDS);
+      } else {
+        // exact slow path: every inner index that some visit range contains
+        const uint32_t innerBegin = lG1[0], innerEnd = lG1[C - 1];
+        for (uint32_t j = innerBegin; j < innerEnd && written < limit; ++j) {
+          bool visited = false;
+          for (uint32_t zs = w.zLowSector; zs < w.zHighSector && !visited; ++zs) {
+            uint32_t a1, b1, a2, b2;
+            pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
+            visited = (a1 <= j && j < b1) || (a2 <= j && j < b2);
+          }
+          if (visited && pair_valid(w, hits[j])) out[written++] = make_uint2(j, i);
+        }
+      }
+      if (written < limit) {
+        atomicAdd(sentinels, limit - written);
+        for (uint32_t q = written; q < limit; ++q) out[q] = make_uint2(TRAX_SENTINEL, TRAX_SENTINEL);
+      }
+    }
+  }
+}
+
+__global__ void pair_offsets_kernel(DevConfig cfg, const uint32_t* taskBase, const uint32_t* pairStart,
+                                    uint32_t* pairOffsets) {
+  const uint32_t S = cfg.E * cfg.nLT;
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= S; s += gridDim.x * blockDim.x)
+    pairOffsets[s] = s == 0 ? 0u : pairStart[taskBase[s]];
+}
+
+int grid_for(uint64_t items, int threads) {
+  uint64_t blocks = (items + threads - 1) / threads;
+  uint64_t cap = (uint64_t)sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+}  // namespace
+
+cudaError_t pair_segments(const DevConfig& cfg, const uint32_t* grid, uint32_t* segOuter, uint32_t* segCount,
+                          cudaStream_t st, uint32_t* launches) {
+  const uint32_t S = cfg.E * cfg.nLT;
+  segments_kernel<<<grid_for(S + 1, 256), 256, 0, st>>>(cfg, grid, segOuter, segCount);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint32_t* segOuter,
+                       const uint32_t* taskBase, const uint32_t* nTasksDev, uint64_t maxTasks, uint32_t* taskCount,
+                       uint2* pairs, uint64_t capPairs, uint32_t* sentinels, uint32_t* err, cudaStream_t st,
+                       uint32_t* launches) {
+  const uint32_t cap = capPairs > 0xffffffffull ? 0xffffffffu : (uint32_t)capPairs;
+  if (maxTasks == 0) return cudaSuccess;
+  const int blocks = grid_for(maxTasks, PAIR_THREADS);
+  if (emit)
+    pair_kernel<true><<<blocks, PAIR_THREADS, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
+                                                       taskCount, pairs, cap, sentinels, err);
+  else
+    pair_kernel<false><<<blocks, PAIR_THREADS, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
+                                                        taskCount, pairs, cap, sentinels, err);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const uint32_t* pairStart,
+                         uint32_t* pairOffsets, cudaStream_t st, uint32_t* launches) {
+  const uint32_t S = cfg.E * cfg.nLT;
+  pair_offsets_kernel<<<grid_for(S + 1, 256), 256, 0, st>>>(cfg, taskBase, pairStart, pairOffsets);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace trax

@@ -1,0 +1,226 @@
+// k_scan.cu -- single-pass exclusive uint32 scan with decoupled look-back,
+// the compaction primitive between the stages (the reference's PrefixSum:
+// PrefixSum.h:58-248 recursive Blelloch scan, PrefixSum.cpp:73-140).
+//
+// One CTA scans one tile of SCAN_THREADS * SCAN_ITEMS elements.  Tiles are
+// numbered by an atomic ticket in launch order, publish their aggregate, and
+// look back over predecessors (a warp reads 32 status words at a time) until
+// one with an inclusive prefix is found.  Every wait is bounded: after
+// TRAX_SPIN_LIMIT polls the tile records TRAX_EBIT_TIMEOUT, treats the
+// missing predecessor as zero and finishes, so a lost tile can never hang
+// the GPU.
+#include "trax_kernels.h"
+
+namespace trax {
+
+namespace {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+constexpr unsigned long long FLAG_AGG = 1ull << 62;
+constexpr unsigned long long FLAG_PREFIX = 2ull << 62;
+
+__device__ __forceinline__ unsigned long long ld_status(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_status(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+    scan_kernel(const uint32_t* __restrict__ in, uint32_t* out, uint64_t nHost, const uint32_t* nDev,
+                uint32_t nAdd, unsigned long long* status, uint32_t* ticket, uint32_t* err) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  __shared__ uint32_t s_prefix;
+  const uint64_t n = nDev ? (uint64_t)(*nDev) + nAdd : nHost;
+  if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint64_t base = (uint64_t)tile * SCAN_TILE;
+  if (base >= n) return;  // successors of this tile do not exist either
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t v[SCAN_ITEMS];
+  const uint64_t i0 = base + (uint64_t)threadIdx.x * SCAN_ITEMS;
+  if (i0 + SCAN_ITEMS <= n && ((reinterpret_cast<uintptr_t>(in) & 15u) == 0)) {
+    const uint4* p = reinterpret_cast<const uint4*>(in + i0);
+    uint4 a = p[0], b = p[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) v[k] = (i0 + k < n) ? in[i0 + k] : 0u;
+  }
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_ITEMS; ++k) {
+    uint32_t t = v[k];
+    v[k] = sum;
+    sum += t;
+  }
+  // block-wide exclusive scan of the per-thread sums
+  uint32_t incl = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = (lane < SCAN_THREADS / 32) ? s_warp[lane] : 0u;
+    uint32_t wi = w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= (uint32_t)d) wi += t;
+    }
+    if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+    uint32_t agg = __shfl_sync(0xffffffffu, wi, SCAN_THREADS / 32 - 1);
+    // publish and look back
+    uint32_t excl = 0;
+    if (tile == 0) {
+      if (lane == 0) st_status(&status[0], FLAG_PREFIX | agg);
+    } else {
+      if (lane == 0) st_status(&status[tile], FLAG_AGG | agg);
+      int64_t pred = (int64_t)tile - 1;
+      uint32_t spins = 0;
+      while (true) {
+        int64_t idx = pred - (int64_t)lane;
+        unsigned long long s = (idx >= 0) ? ld_status(&status[idx]) : (FLAG_PREFIX | 0ull);
+        unsigned long long flag = s & (3ull << 62);
+        if (__any_sync(0xffffffffu, flag == 0ull)) {
+          if (++spins < TRAX_SPIN_LIMIT) {
+            __nanosleep(64);
+            continue;
+          }
+          // bounded wait ran out: record it and treat the missing tiles as empty
+          if (lane == 0) raise_error(err, TRAX_EBIT_TIMEOUT);
+          if (flag == 0ull) s = FLAG_AGG;
+          flag = s & (3ull << 62);
+        }
+        uint32_t val = (uint32_t)(s & 0xffffffffull);
+        uint32_t pmask = __ballot_sync(0xffffffffu, flag == FLAG_PREFIX);
+        if (pmask) {
+          uint32_t first = __ffs(pmask) - 1;
+          uint32_t contrib = (lane <= first) ? val : 0u;
+#pragma unroll
+          for (int d = 16; d > 0; d >>= 1) contrib += __shfl_down_sync(0xffffffffu, contrib, d);
+          excl += __shfl_sync(0xffffffffu, contrib, 0);
+          break;
+        }
+        uint32_t contrib = val;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) contrib += __shfl_down_sync(0xffffffffu, contrib, d);
+        excl += __shfl_sync(0xffffffffu, contrib, 0);
+        pred -= 32;
+      }
+      if (lane == 0) st_status(&status[tile], FLAG_PREFIX | (uint32_t)(excl + agg));
+    }
+    if (lane == 0) s_prefix = excl;
+  }
+  __syncthreads();
+  const uint32_t off = s_prefix + s_warp[warp] + (incl - sum);
+  if (i0 + SCAN_ITEMS <= n && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
+    uint4* p = reinterpret_cast<uint4*>(out + i0);
+    p[0] = make_uint4(off + v[0], off + v[1], off + v[2], off + v[3]);
+    p[1] = make_uint4(off + v[4], off + v[5], off + v[6], off + v[7]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+      if (i0 + k < n) out[i0 + k] = off + v[k];
+  }
+}
+
+// Inclusive running maximum, one CTA (the serial semantics of the offset
+// monotonize kernels, TripletThetaPhiFilter.h:267-280).
+__global__ void __launch_bounds__(1024) max_scan_kernel(uint32_t* data, uint32_t n) {
+  __shared__ uint32_t s_w[32];
+  __shared__ uint32_t s_carry;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (uint32_t b = 0; b < n; b += blockDim.x) {
+    uint32_t i = b + threadIdx.x;
+    uint32_t v = i < n ? data[i] : 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
+      if (lane >= (uint32_t)d) v = max(v, t);
+    }
+    if (lane == 31) s_w[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = (lane < blockDim.x / 32) ? s_w[lane] : 0u;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, w, d);
+        if (lane >= (uint32_t)d) w = max(w, t);
+      }
+      s_w[lane] = w;
+    }
+    __syncthreads();
+    uint32_t pre = (warp > 0) ? s_w[warp - 1] : 0u;
+    uint32_t r = max(max(v, pre), s_carry);
+    if (i < n) data[i] = r;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) s_carry = r;
+    __syncthreads();
+  }
+}
+
+// dst = data[n] with n = *nDev (or nHost), clamped to cap
+__global__ void publish_kernel(const uint32_t* data, const uint32_t* nDev, uint32_t nHost, uint32_t cap,
+                               uint32_t* dst, uint32_t* err) {
+  const uint32_t n = nDev ? *nDev : nHost;
+  uint32_t v = data[n];
+  if (v > cap) {
+    v = cap;
+    raise_error(err, TRAX_EBIT_CAPACITY);
+  }
+  *dst = v;
+}
+
+}  // namespace
+
+cudaError_t publish_total(const uint32_t* data, const uint32_t* nDev, uint64_t nHost, uint64_t cap, uint32_t* dst,
+                          uint32_t* err, cudaStream_t st, uint32_t* launches) {
+  const uint32_t c = cap > 0xffffffffull ? 0xffffffffu : (uint32_t)cap;
+  publish_kernel<<<1, 1, 0, st>>>(data, nDev, (uint32_t)nHost, c, dst, err);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+size_t scan_scratch_bytes(uint64_t maxN) {
+  uint64_t tiles = (maxN + SCAN_TILE - 1) / SCAN_TILE + 1;
+  return 256 + tiles * sizeof(unsigned long long);
+}
+
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const uint32_t* nDev, uint32_t nAdd,
+                           uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches) {
+  uint64_t cap = nDev ? maxN : n;
+  if (cap == 0) return cudaSuccess;
+  uint64_t tiles = (cap + SCAN_TILE - 1) / SCAN_TILE;
+  size_t bytes = 256 + tiles * sizeof(unsigned long long);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, bytes, st);
+  if (e != cudaSuccess) return e;
+  uint32_t* ticket = reinterpret_cast<uint32_t*>(scratch);
+  unsigned long long* status = reinterpret_cast<unsigned long long*>(static_cast<char*>(scratch) + 256);
+  scan_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, out, n, nDev, nAdd, status, ticket, err);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* launches) {
+  if (n == 0) return cudaSuccess;
+  max_scan_kernel<<<1, 1024, 0, st>>>(data, n);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+}  // namespace trax

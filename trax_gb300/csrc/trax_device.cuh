@@ -1,0 +1,69 @@
+// trax_device.cuh -- device-side configuration, error reporting and the
+// primitives shared by the sm_103a kernels of the triplet-seeding path.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "trax_math.h"
+
+namespace trax {
+
+#define TRAX_MAX_LT 16
+#define TRAX_MAX_LAYERS 32
+#define TRAX_SENTINEL 0xffffffffu
+
+// error bits written by kernels into the context's device error word
+#define TRAX_EBIT_TIMEOUT 1u
+#define TRAX_EBIT_CAPACITY 2u
+#define TRAX_EBIT_BOUNDS 4u
+
+// Everything a kernel needs to know about the workload, passed by value.
+struct DevConfig {
+  uint32_t E, L, nZ, nP, C, nLT;
+  float minZ, sZ, minPhi, sP;
+  float minRcurv;
+  float dEtaCut;
+  uint32_t layer1[TRAX_MAX_LT], layer2[TRAX_MAX_LT], layer3[TRAX_MAX_LT];
+  float dThetaCut[TRAX_MAX_LT], sigmaZ[TRAX_MAX_LT], dPhiCut[TRAX_MAX_LT];
+  float sigmaPhi[TRAX_MAX_LT], tipCut[TRAX_MAX_LT], z0[TRAX_MAX_LT];
+  float pairSigmaPhi[TRAX_MAX_LT];  // pairSpreadPhi bit pattern read as float
+  float minR[TRAX_MAX_LAYERS], maxR[TRAX_MAX_LAYERS];
+};
+
+// Grid-ordered hit collection (the reference's HitCollection after GridBuilder).
+struct DevHits {
+  float* x;
+  float* y;
+  float* z;
+  uint32_t* layer;
+  uint32_t* det;
+  uint32_t* hid;
+  uint32_t* evt;
+  uint32_t* orig;  // index of the hit in the uploaded input
+  float4* xyzp;    // packed (x, y, z, phi) for the candidate loops
+};
+
+__device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) {
+  if (err) atomicOr(err, bit);
+}
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Layer-local grid read clamped to the last cell of the layer (the reference
+// reads past the layer for NaN/inf windows; both sides clamp).
+__device__ __forceinline__ uint32_t cell_at(const uint32_t* lGrid, uint32_t k, uint32_t C) {
+  return lGrid[k < C ? k : C - 1];
+}
+
+// Maximum number of polls of a predecessor's scan status before a tile gives
+// up, records TRAX_EBIT_TIMEOUT and carries on with what it has.
+#define TRAX_SPIN_LIMIT (1u << 22)
+
+}  // namespace trax

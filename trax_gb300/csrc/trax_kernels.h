@@ -1,0 +1,137 @@
+// trax_kernels.h -- host-side launchers of the sm_103a kernels.  Each
+// launcher enqueues work on `st` and adds the number of kernels it launched
+// to *launches.  Counts that are only known on the device are passed as
+// device pointers together with a host-side capacity that sizes the grid.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "trax_device.cuh"
+
+namespace trax {
+
+// ---------------------------------------------------------------- scans
+size_t scan_scratch_bytes(uint64_t maxN);
+// Exclusive scan of n elements (or *nDev + nAdd when nDev != nullptr, with
+// maxN bounding the launch), in place allowed.
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const uint32_t* nDev, uint32_t nAdd,
+                           uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches);
+cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* launches);
+
+// ------------------------------------------------------------ grid build
+struct GridInput {
+  const float* x;
+  const float* y;
+  const float* z;
+  const uint32_t* layer;
+  const uint32_t* det;
+  const uint32_t* hid;
+  const uint32_t* evt;
+  const uint32_t* eventOffsets;  // [E]
+  const uint32_t* layerHits;     // [E*L]
+  const uint32_t* layerOffsets;  // [E*L]
+};
+
+struct GridScratch {
+  uint32_t* cell;    // [n]
+  float* phi;        // [n]
+  uint32_t* perm;    // [n]
+  uint32_t* counts;  // [E*L*C] used when the cell counters do not fit in shared memory
+};
+
+cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid, DevHits out,
+                       GridScratch scratch, uint32_t* err, cudaStream_t st, uint32_t* launches);
+cudaError_t grid_prepare(int device);  // one-time kernel attributes
+
+// ----------------------------------------------------------------- pairs
+// Per (event, layer triplet) segment: first outer hit and number of outer hits.
+cudaError_t pair_segments(const DevConfig& cfg, const uint32_t* grid, uint32_t* segOuter, uint32_t* segCount,
+                          cudaStream_t st, uint32_t* launches);
+// Count (emit == false) or store (emit == true) pairs of every outer-hit task.
+// taskBase[S+1] is the exclusive scan of segCount; nTasksDev = &taskBase[S].
+cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits,
+                       const uint32_t* segOuter, const uint32_t* taskBase, const uint32_t* nTasksDev,
+                       uint64_t maxTasks, uint32_t* taskCount, uint2* pairs, uint64_t capPairs,
+                       uint32_t* sentinelCount, uint32_t* err, cudaStream_t st, uint32_t* launches);
+// pairOffsets[s+1] = first pair of segment s+1 (Pairing::pairingOffsets)
+cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const uint32_t* pairStart,
+                         uint32_t* pairOffsets, cudaStream_t st, uint32_t* launches);
+
+// ------------------------------------------------------------ prediction
+cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
+                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint2* cands,
+                          uint64_t capCands, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
+                          uint32_t* launches);
+cudaError_t predict_offsets(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint32_t* nPairsDev,
+                            uint64_t maxPairs, const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st,
+                            uint32_t* launches);
+
+// ---------------------------------------------------------------- filter
+cudaError_t filter_candidates(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint2* cands,
+                              const uint32_t* nCandsDev, uint64_t maxCands, uint32_t* flags, cudaStream_t st,
+                              uint32_t* launches);
+cudaError_t filter_store(const uint2* pairs, const uint2* cands, const uint32_t* nCandsDev, uint64_t maxCands,
+                         const uint32_t* flagScan, uint32_t* h1, uint32_t* h2, uint32_t* h3, uint64_t capT,
+                         cudaStream_t st, uint32_t* launches);
+// trackletOffsets with the reference's filterOffsetStore + monotonize semantics
+cudaError_t triplet_offsets(const DevConfig& cfg, DevHits hits, const uint32_t* h1, const uint32_t* nTDev,
+                            uint64_t maxT, uint32_t* offsets, cudaStream_t st, uint32_t* launches);
+
+// ---------------------------------------------------------- connectivity
+struct TripletView {
+  const uint32_t* h1;
+  const uint32_t* h2;
+  const uint32_t* h3;
+  const uint32_t* nDev;
+  uint64_t maxN;
+};
+
+cudaError_t triplet_eta(const DevConfig& cfg, DevHits hits, TripletView t, float* eta, uint32_t* seg,
+                        cudaStream_t st, uint32_t* launches);
+cudaError_t segment_bounds(const DevConfig& cfg, const uint32_t* seg, const uint32_t* nTDev, uint32_t* segStart,
+                           cudaStream_t st, uint32_t* launches);
+cudaError_t connectivity_tasks(const DevConfig& cfg, bool emit, DevHits hits, TripletView t, const float* eta,
+                               const uint32_t* offsets, const uint32_t* segStart, uint32_t* linkCount,
+                               uint32_t* flags, uint32_t* basis, uint32_t* follower, uint64_t capLinks,
+                               cudaStream_t st, uint32_t* launches);
+// flags[k] for k < n-1 -> (flag, !flag) streams for the two compactions; element n-1 and the +1 slot are 0
+cudaError_t connectable_streams(const uint32_t* flags, const uint32_t* nTDev, uint64_t maxT, uint32_t* conn,
+                                uint32_t* nonConn, cudaStream_t st, uint32_t* launches);
+cudaError_t compact_indices(const uint32_t* scan, const uint32_t* nTDev, uint64_t maxT, uint32_t* outIdx,
+                            uint64_t capOut, cudaStream_t st, uint32_t* launches);
+// *dst = data[n] (n = *nDev, or nHost when nDev is null): the total a scan of
+// n+1 elements left in its last slot, clamped to cap (TRAX_EBIT_CAPACITY)
+cudaError_t publish_total(const uint32_t* data, const uint32_t* nDev, uint64_t nHost, uint64_t cap, uint32_t* dst,
+                          uint32_t* err, cudaStream_t st, uint32_t* launches);
+
+// ---------------------------------------------------- circle fit and CA
+cudaError_t circle_fit(DevHits hits, TripletView t, const uint32_t* connectable, const uint32_t* nConnDev,
+                       uint64_t maxConn, float* pt, cudaStream_t st, uint32_t* launches);
+
+struct CABuffers {
+  uint32_t* states;    // [nT]
+  uint32_t* inStart;   // [nT+1]
+  uint32_t* inCursor;  // [nT]
+  uint32_t* inList;    // [nLinks] link indices grouped by follower
+  uint32_t* best;      // [nT]
+  uint32_t* isBest;    // [nT]
+  uint32_t* handlers;  // [nT+1]
+  uint32_t* segOf;     // [nT] layer-triplet segment of each triplet
+};
+
+cudaError_t ca_in_degree(const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks, CABuffers b,
+                         const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches);
+cudaError_t ca_fill(const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks, CABuffers b,
+                    const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches);
+cudaError_t ca_forward(const DevConfig& cfg, const uint32_t* basis, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
+                       cudaStream_t st, uint32_t* launches);
+cudaError_t ca_backward(const uint32_t* basis, const float* pt, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
+                        const uint32_t* nLinksDev, cudaStream_t st, uint32_t* launches);
+cudaError_t ca_tracks(CABuffers b, const uint32_t* nTDev, uint64_t maxT, uint32_t* tracks, uint64_t maxTracks,
+                      uint32_t* err, cudaStream_t st, uint32_t* launches);
+
+// number of SMs of the current device (cached)
+int sm_count();
+
+}  // namespace trax
