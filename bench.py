@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark of the triplet-seeding chain on GB300.
+
+Workload: 1000 ttbar-like events with uneven sizes (tracks ~ Poisson(lambda),
+lambda ~ U[300, 3000]; 10 barrel layers, 6 layer triplets), seeded synthetic
+data (the reference's own event files are not distributed).  One step is the
+whole chain -- grid build, pairs, prediction, filter, connectivity, circle fit,
+cellular automaton -- over the full batch, replayed from a CUDA graph.
+
+value      events/s with the hits already resident in HBM, device time from
+           CUDA events around each graph launch (inputs: ~270 MB of hits,
+           larger than the 129 MB L2, so no L2 flush is needed between steps)
+e2e        the same metric through the C ABI from host buffers: upload of the
+           hit columns, the chain, and the download of the triplets and tracks
+           inside the timed region (host wall clock, synchronized)
+plain      the per-event launch structure of the reference (one event per
+           stage call, host-synced count/scan/store) over the first events
+roofline   the dominant kernel's algorithmic bytes / its CUDA-event time
+           against the measured HBM copy bandwidth
+cpu_baseline  the CPU oracle (a restatement of the reference kernels; the
+           reference's OpenCL build cannot run here) on a bounded sample
+
+Multi-GPU (torchrun): every rank processes its own 1000-event batch on its
+own GPU (events are independent; no collective on the data path); value is
+all ranks' events over the slowest rank's time.
+
+--impl reference times the CPU restatement of the reference on the host
+cores instead (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "events/s & triplets/s on 1 GB300, batched vs per-event, bit-exact triplet sets"
+CONFIG = 2
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--events", type=int, default=1000)
+    p.add_argument("--plain-events", type=int, default=48)
+    p.add_argument("--cpu-sample", type=int, default=128)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--no-plain", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-parity", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ ranks
+class Ranks:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) != len(self.FIELDS):
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if parts[5 + k].lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_baseline(batch, n_events: int):
+    from oracle import oracle
+    sample = batch.subset(range(min(n_events, batch.n_events)))
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    res = oracle.run(sample, event_grouping=1, n_workers=cores)
+    dt = time.perf_counter() - t0
+    trip = sum(r["stats_dict"]["triplets"] for r in res)
+    return {"value": round(sample.n_events / dt, 3), "unit": "events/s", "cores": cores, "kind": "port",
+            "sample": f"first {sample.n_events} events of the 1000-event workload, one event per group, "
+                      f"{cores} host threads, {dt:.2f} s wall",
+            "triplets_per_s": round(trip / dt, 1)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# Algorithmic bytes of the timed kernels: compulsory streams only (each input
+# array read once, each output written once), from the sizes of the run.
+def kernel_bytes(name, st, n_tasks, n_hits, cells):
+    P, Cc, T = st.n_pairs, st.n_candidates, st.n_triplets
+    return {
+        "grid_build": 56 * n_hits + 4 * cells,
+        "pair_count": 16 * n_tasks + 4 * n_tasks,
+        "pair_store": 16 * n_tasks + 8 * n_tasks + 8 * P,
+        "predict_count": 8 * P + 4 * P,
+        "predict_store": 8 * P + 8 * P + 8 * Cc,
+        "filter": 8 * Cc + 4 * Cc,
+        "filter_store": 8 * Cc + 8 * Cc + 12 * T,
+        "connectivity_count": 12 * T + 4 * T + 4 * T,
+        "connectivity_store": 12 * T + 8 * st.n_links,
+    }.get(name, 0)
+
+
+def chain_bytes(st, n_hits, cells, n_layers):
+    # SURVEY-style per-batch algorithmic bytes of the whole chain
+    P, Cc, T, Lk = st.n_pairs, st.n_candidates, st.n_triplets, st.n_links
+    return (56 * n_hits + 4 * cells + 16 * P + 16 * Cc + 24 * T + 4 * T + 16 * Lk + 8 * st.n_connectable
+            + (8 * Lk + 8 * T) * max(1, n_layers))
+
+
+def run_plain(ctx, batch, n_events):
+    """Reference launch structure: one event per call, every stage host-synced."""
+    from trax_gb300 import capi  # noqa: F401
+    times = []
+    trip = 0
+    for e in range(min(n_events, batch.n_events)):
+        sub = batch.subset([e])
+        ctx.upload(sub)
+        t0 = time.perf_counter()
+        ctx.grid_build()
+        ctx.pair_gen()
+        ctx.triplet_predict()
+        trip += ctx.triplet_filter()
+        if ctx.connectivity(batch.d_eta_cut):
+            ctx.circle_fit()
+            ctx.cellular_automaton()
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    return {"value": round(len(times) / total, 2), "unit": "events/s", "events": len(times),
+            "triplets_per_s": round(trip / total, 1),
+            "structure": "one event per stage call; host-synced count -> scan -> read total -> store"}
+
+
+def parity_sample(ctx, batch, n=6):
+    from oracle import oracle
+    sub = batch.subset(range(n))
+    ref = oracle.run(sub)[0]
+    ctx.upload(sub)
+    ctx.seed_batch(use_graph=True)
+    got = ctx.results()
+    ok = all(np.array_equal(np.asarray(got[k]), np.asarray(ref[k]))
+             for k in ("pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "link_basis", "link_follower", "tracks"))
+    return f"{'bit-exact' if ok else 'MISMATCH'} against the CPU oracle on the first {n} events"
+
+
+def run_ours(args, ranks: Ranks):
+    from trax_gb300 import capi, events
+    device = ranks.local
+    seed = 2 + 1000 * ranks.rank
+    batch = events.generate(CONFIG, n_events=args.events, seed=seed)
+    n_hits = batch.n_hits
+    cells = batch.n_events * batch.n_layers * (batch.n_z + 1) * (batch.n_phi + 1)
+    ctx = capi.Context(device)
+    ctx.upload(batch)
+    for _ in range(max(args.warmup, 3)):
+        st = ctx.seed_batch(use_graph=True)
+    clocks = ClockSampler(device)
+    ranks.barrier()
+    clocks.start()
+    dev_ms = []
+    kern = {k: [] for k in capi.Context.KERNELS}
+    stage = {k: [] for k in capi.Context.STAGES}
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = ctx.seed_batch(use_graph=True)
+        dev_ms.append(st.device_ms)
+        s_ms, k_ms = ctx.timings()
+        for k, v in k_ms.items():
+            kern[k].append(v)
+        for k, v in s_ms.items():
+            stage[k].append(v)
+    t_wall = time.perf_counter() - t_wall0
+    clk = clocks.stop()
+    ranks.barrier()
+    my_time = sum(dev_ms) / 1e3
+    t_max = ranks.max(my_time)
+    events_all = ranks.sum(float(batch.n_events * args.steps))
+    trip_all = ranks.sum(float(st.n_triplets * args.steps))
+    value = events_all / t_max
+    ms_per_step = 1e3 * t_max / args.steps
+    launches = st.kernel_launches * args.steps
+
+    # roofline of the dominant kernel (mean CUDA-event time over the steps)
+    kmean = {k: float(np.mean(v)) for k, v in kern.items() if v and min(v) >= 0}
+    if not kmean:
+        raise RuntimeError("no per-kernel CUDA-event timings were recorded")
+    dom = max(kmean, key=kmean.get)
+    # pair-stage tasks: one per outer-layer hit of every (event, layer triplet)
+    n_tasks = int(sum(int(batch.layer_hits[:, lt.layer2 - 1].sum()) for lt in batch.lts))
+    hbm, peak_kind = peaks()
+    kb = kernel_bytes(dom, st, n_tasks, n_hits, cells)
+    achieved = kb / (kmean[dom] * 1e-3) / 1e9
+    cb = chain_bytes(st, n_hits, cells, len(batch.lts))
+    result = {
+        "metric": METRIC, "value": round(value, 2), "unit": "events/s", "n_gpus": ranks.world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "ttbar-like batch: 1000 events, tracks ~ Poisson(U[300,3000]), 10 layers, 6 layer "
+                               "triplets, seed 2 (config 2)",
+                   "events_per_gpu": batch.n_events, "hits_per_gpu": n_hits, "grid": f"{batch.n_z}x{batch.n_phi}",
+                   "layer_triplets": len(batch.lts),
+                   "l2": f"inputs larger than L2 ({n_hits * 28 / 1e6:.0f} MB of hit columns per step), no flush",
+                   "path": "batched: one CUDA-graph replay of the whole chain per step"},
+        "triplets_per_s": round(trip_all / t_max, 1),
+        "sizes": {"pairs": st.n_pairs, "candidates": st.n_candidates, "triplets": st.n_triplets,
+                  "links": st.n_links, "track_entries": st.n_track_entries},
+        "stage_ms": {k: round(float(np.mean(v)), 4) for k, v in stage.items() if v and min(v) >= 0},
+        "kernel_ms": {k: round(v, 4) for k, v in kmean.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
+                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "peak_kind": f"{peak_kind} hbm_gbs (copy bandwidth)",
+                     "algorithmic_bytes": int(kb)},
+        "chain_roofline": {"achieved": round(cb / (ms_per_step * 1e-3) / 1e9, 2), "unit": "GB/s",
+                           "frac": round(cb / (ms_per_step * 1e-3) / 1e9 / hbm, 4), "bytes_per_step": int(cb)},
+        "gpu_launches": int(launches),
+        "wall_s": round(t_wall, 3),
+        "clocks": clk,
+    }
+
+    # end to end through the C ABI from host buffers
+    if ranks.rank == 0 or True:
+        e2e_times = []
+        bi = int(sum(getattr(batch, k).nbytes for k in ("x", "y", "z", "layer", "det_id", "hit_id", "event"))
+                 + batch.event_offsets.nbytes + batch.layer_hits.nbytes + batch.layer_offsets.nbytes)
+        bo = 0
+        for it in range(args.e2e_steps + 1):
+            t0 = time.perf_counter()
+            ctx.upload_hits(batch)
+            s2 = ctx.seed_batch(use_graph=True)
+            h1, h2, h3, _ = ctx.triplets()
+            _, tr, toff = ctx.tracks()
+            dt = time.perf_counter() - t0
+            bo = int(h1.nbytes + h2.nbytes + h3.nbytes + tr.nbytes + toff.nbytes)
+            if it > 0:
+                e2e_times.append(dt)
+        e2e_t = ranks.max(sum(e2e_times))
+        e2e_events = ranks.sum(float(batch.n_events * len(e2e_times)))
+        result["e2e"] = {"value": round(e2e_events / e2e_t, 2), "unit": "events/s", "h2d_bytes_per_step": bi,
+                         "d2h_bytes_per_step": bo, "steps": len(e2e_times),
+                         "note": "pageable host arrays; upload + graph replay + triplet/track download, wall clock"}
+    if ranks.rank == 0:
+        if not args.no_plain:
+            plain = run_plain(ctx, batch, args.plain_events)
+            result["plain_per_event"] = plain
+            result["batched_over_plain"] = round(value / ranks.world / plain["value"], 2)
+        if not args.no_parity:
+            result["parity"] = parity_sample(ctx, batch)
+        if not args.no_cpu:
+            result["cpu_baseline"] = cpu_baseline(batch, args.cpu_sample)
+    ctx.close()
+    return result
+
+
+def run_reference(args, ranks: Ranks):
+    if ranks.rank != 0:
+        return None
+    from oracle import oracle
+    from trax_gb300 import events
+    batch = events.generate(CONFIG, n_events=args.events)
+    cores = os.cpu_count() or 1
+    per_step = max(cores, 32)
+    warm = batch.subset(range(min(8, batch.n_events)))
+    for _ in range(max(args.warmup, 3)):
+        oracle.run(warm, event_grouping=1, n_workers=cores)
+    times, evs, trip = [], 0, 0
+    for k in range(args.steps):
+        lo = (k * per_step) % max(1, batch.n_events - per_step)
+        sample = batch.subset(range(lo, lo + per_step))
+        t0 = time.perf_counter()
+        res = oracle.run(sample, event_grouping=1, n_workers=cores)
+        times.append(time.perf_counter() - t0)
+        evs += sample.n_events
+        trip += sum(r["stats_dict"]["triplets"] for r in res)
+    total = sum(times)
+    v = round(evs / total, 3)
+    return {
+        "metric": METRIC, "impl": "reference", "value": v, "unit": "events/s", "n_gpus": ranks.world,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "ttbar-like batch: 1000 events, tracks ~ Poisson(U[300,3000]), 10 layers, 6 layer "
+                               "triplets, seed 2 (config 2)", "events_per_step": per_step},
+        "triplets_per_s": round(trip / total, 1),
+        "cpu_baseline": {"value": v, "unit": "events/s", "cores": cores, "kind": "port",
+                         "sample": f"{per_step} events per step of the 1000-event workload, one event per group; "
+                                   "CPU restatement of the reference kernels (the reference's OpenCL build "
+                                   "cannot run: empty clever submodule, no OpenCL ICD)"},
+        "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    ranks = Ranks()
+    try:
+        if args.impl == "reference":
+            res = run_reference(args, ranks)
+        else:
+            res = run_ours(args, ranks)
+        if ranks.rank == 0 and res is not None:
+            print(json.dumps(res), flush=True)
+    finally:
+        ranks.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -149,6 +149,14 @@ int trax_prefix_sum(trax_ctx* ctx, uint32_t* data, uint64_t n);
  * CUDA graph. */
 int trax_seed_batch(trax_ctx* ctx, const trax_batch_opts* opts, trax_batch_stats* stats);
 
+/* Device time of the last run, from CUDA events on the context's stream
+ * (RuntimeRecord's per-stage count/scan/store classes, RuntimeRecord.cpp:123-192):
+ * stage_ms[7] = grid, pairs, prediction, filter, connectivity, circle fit, CA;
+ * kernel_ms[9] = grid build, pair count, pair store, prediction count,
+ * prediction store, filter, filter store, connectivity count, connectivity
+ * store.  Entries that did not run are -1. */
+int trax_get_timings(trax_ctx* ctx, float* stage_ms, float* kernel_ms);
+
 /* ------------------------------------------------------------- results
  * Sizes first (*_size), then copies into caller-allocated host buffers. */
 int trax_get_stats(trax_ctx* ctx, trax_batch_stats* stats);

@@ -26,7 +26,7 @@ EXPORTED = [
     "trax_set_geometry", "trax_set_grid", "trax_upload_hits", "trax_grid_build", "trax_pair_gen",
     "trax_triplet_predict", "trax_triplet_filter", "trax_connectivity", "trax_circle_fit",
     "trax_cellular_automaton", "trax_prefix_sum", "trax_seed_batch", "trax_get_stats", "trax_get_pairs",
-    "trax_get_candidates", "trax_get_triplets", "trax_get_triplet_eta_pt", "trax_get_links",
+    "trax_get_timings", "trax_get_candidates", "trax_get_triplets", "trax_get_triplet_eta_pt", "trax_get_links",
     "trax_get_tracks", "trax_get_grid", "trax_get_hit_perm",
 ]
 
@@ -101,6 +101,7 @@ def load() -> ctypes.CDLL:
             "trax_prefix_sum": ([vp, vp, u64], i32),
             "trax_seed_batch": ([vp, vp, vp], i32),
             "trax_get_stats": ([vp, vp], i32),
+            "trax_get_timings": ([vp, vp, vp], i32),
             "trax_get_pairs": ([vp, vp, vp], i32),
             "trax_get_candidates": ([vp, vp, vp], i32),
             "trax_get_triplets": ([vp, vp, vp, vp, vp], i32),
@@ -252,6 +253,17 @@ class Context:
         st = BatchStatsC()
         self._check(self._L.trax_get_stats(self._h, ctypes.byref(st)))
         return BatchStats(*[getattr(st, f[0]) for f in BatchStatsC._fields_])
+
+    STAGES = ["grid", "pairs", "predict", "filter", "connectivity", "circle_fit", "ca"]
+    KERNELS = ["grid_build", "pair_count", "pair_store", "predict_count", "predict_store", "filter",
+               "filter_store", "connectivity_count", "connectivity_store"]
+
+    def timings(self):
+        """(stage ms, kernel ms) of the last run, from CUDA events; -1 = not run."""
+        s = np.zeros(len(self.STAGES), dtype=np.float32)
+        k = np.zeros(len(self.KERNELS), dtype=np.float32)
+        self._check(self._L.trax_get_timings(self._h, _p(s), _p(k)))
+        return dict(zip(self.STAGES, s.tolist())), dict(zip(self.KERNELS, k.tolist()))
 
     def prefix_sum(self, data: np.ndarray) -> np.ndarray:
         a = np.ascontiguousarray(data, dtype=np.uint32).copy()

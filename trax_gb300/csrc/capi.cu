@@ -71,6 +71,21 @@ enum Slot {
 
 enum Mode { SYNCED, DEVICE };
 
+// kernels timed individually with CUDA events (order of trax_get_timings)
+enum TimedKernel {
+  TK_GRID = 0,
+  TK_PAIR_COUNT,
+  TK_PAIR_EMIT,
+  TK_PRED_COUNT,
+  TK_PRED_EMIT,
+  TK_FILTER,
+  TK_FILTER_STORE,
+  TK_CONN_COUNT,
+  TK_CONN_EMIT,
+  TK_N
+};
+const int N_STAGES = 7;
+
 const uint64_t NO_CAP = 0xffffffffull;
 
 }  // namespace
@@ -118,6 +133,11 @@ struct trax_ctx {
   uint32_t graphLaunches = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double lastMs = 0.0;
+  // per-stage and per-kernel timing events of the last run
+  cudaEvent_t stageEv[N_STAGES + 1] = {};
+  cudaEvent_t kEv[2 * TK_N] = {};
+  bool stageUsed[N_STAGES] = {};
+  bool kUsed[TK_N] = {};
 };
 
 namespace {
@@ -187,6 +207,24 @@ DevHits dev_hits(trax_ctx* c) {
 }
 
 uint32_t* slot(trax_ctx* c, int k) { return ptr<uint32_t>(c->slots) + k; }
+
+// event marks around one kernel (recorded into the graph when capturing)
+// While the stream is being captured the record becomes an event-record node
+// of the graph (cudaEventRecordExternal); otherwise it is a plain record.
+cudaError_t record(trax_ctx* c, cudaEvent_t ev) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(c->st, &cs);
+  if (e != cudaSuccess) return e;
+  if (cs == cudaStreamCaptureStatusActive) return cudaEventRecordWithFlags(ev, c->st, cudaEventRecordExternal);
+  return cudaEventRecord(ev, c->st);
+}
+
+void kmark(trax_ctx* c, int k, bool end) {
+  record(c, c->kEv[2 * k + (end ? 1 : 0)]);
+  if (end) c->kUsed[k] = true;
+}
+#define KBEG(k) kmark(c, k, false)
+#define KEND(k) kmark(c, k, true)
 uint32_t* dev_err(trax_ctx* c) { return slot(c, S_ERR); }
 
 float min_radius_curvature(float minPt) {
@@ -317,7 +355,9 @@ int stage_grid(trax_ctx* c, Mode mode) {
   sc.phi = ptr<float>(c->sc_phi);
   sc.perm = ptr<uint32_t>(c->sc_perm);
   sc.counts = ptr<uint32_t>(c->sc_counts);
+  KBEG(TK_GRID);
   CK(grid_build(c->cfg, in, ptr<uint32_t>(c->grid), dev_hits(c), sc, dev_err(c), c->st, &c->launches));
+  KEND(TK_GRID);
   return TRAX_OK;
 }
 
@@ -337,8 +377,10 @@ int stage_pairs(trax_ctx* c, Mode mode) {
   }
   ENSURE(taskCount, maxTasks + 1, 4);
   uint32_t* taskCount = ptr<uint32_t>(c->taskCount);
+  KBEG(TK_PAIR_COUNT);
   CK(pair_tasks(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
                 maxTasks, taskCount, nullptr, 0, slot(c, S_PAIR_SENT), dev_err(c), c->st, &c->launches));
+  KEND(TK_PAIR_COUNT);
   RC(scan_publish(c, mode, taskCount, c->nTasks, mode == DEVICE ? nTasksDev : nullptr, maxTasks, S_PAIRS,
                   mode == DEVICE ? c->capPairs : NO_CAP));
   uint64_t maxPairs = c->capPairs;
@@ -347,9 +389,11 @@ int stage_pairs(trax_ctx* c, Mode mode) {
     maxPairs = c->nPairs;
   }
   ENSURE(pairs, maxPairs, 8);
+  KBEG(TK_PAIR_EMIT);
   CK(pair_tasks(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
                 maxTasks, taskCount, ptr<uint2>(c->pairs), maxPairs, slot(c, S_PAIR_SENT), dev_err(c), c->st,
                 &c->launches));
+  KEND(TK_PAIR_EMIT);
   CK(pair_offsets(c->cfg, taskBase, taskCount, ptr<uint32_t>(c->pairOffsets), c->st, &c->launches));
   return TRAX_OK;
 }
@@ -361,8 +405,10 @@ int stage_predict(trax_ctx* c, Mode mode) {
   ENSURE(candCount, maxPairs + 1, 4);
   ENSURE(candOffsets, S + 1, 4);
   uint32_t* candCount = ptr<uint32_t>(c->candCount);
+  KBEG(TK_PRED_COUNT);
   CK(predict_pairs(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
                    candCount, nullptr, 0, slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+  KEND(TK_PRED_COUNT);
   RC(scan_publish(c, mode, candCount, c->nPairs, mode == DEVICE ? nPairsDev : nullptr, maxPairs, S_CANDS,
                   mode == DEVICE ? c->capCands : NO_CAP));
   uint64_t maxCands = c->capCands;
@@ -371,8 +417,10 @@ int stage_predict(trax_ctx* c, Mode mode) {
     maxCands = c->nCands;
   }
   ENSURE(cands, maxCands, 8);
+  KBEG(TK_PRED_EMIT);
   CK(predict_pairs(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
                    candCount, ptr<uint2>(c->cands), maxCands, slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+  KEND(TK_PRED_EMIT);
   CK(predict_offsets(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs, candCount,
                      ptr<uint32_t>(c->candOffsets), c->st, &c->launches));
   return TRAX_OK;
@@ -385,8 +433,10 @@ int stage_filter(trax_ctx* c, Mode mode) {
   ENSURE(flags, maxCands + 1, 4);
   ENSURE(tripOffsets, S + 1, 4);
   uint32_t* flags = ptr<uint32_t>(c->flags);
+  KBEG(TK_FILTER);
   CK(filter_candidates(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, flags,
                        c->st, &c->launches));
+  KEND(TK_FILTER);
   RC(scan_publish(c, mode, flags, c->nCands, mode == DEVICE ? nCandsDev : nullptr, maxCands, S_TRIPLETS,
                   mode == DEVICE ? c->capT : NO_CAP));
   uint64_t maxT = c->capT;
@@ -397,8 +447,10 @@ int stage_filter(trax_ctx* c, Mode mode) {
   ENSURE(h1, maxT, 4);
   ENSURE(h2, maxT, 4);
   ENSURE(h3, maxT, 4);
+  KBEG(TK_FILTER_STORE);
   CK(filter_store(ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, flags, ptr<uint32_t>(c->h1),
                   ptr<uint32_t>(c->h2), ptr<uint32_t>(c->h3), maxT, c->st, &c->launches));
+  KEND(TK_FILTER_STORE);
   CK(triplet_offsets(c->cfg, dev_hits(c), ptr<uint32_t>(c->h1), slot(c, S_TRIPLETS), maxT,
                      ptr<uint32_t>(c->tripOffsets), c->st, &c->launches));
   return TRAX_OK;
@@ -436,9 +488,11 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
   CK(triplet_eta(c->cfg, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->segOf), c->st, &c->launches));
   CK(segment_bounds(c->cfg, ptr<uint32_t>(c->segOf), nTDev, ptr<uint32_t>(c->segStart), c->st, &c->launches));
   uint32_t* linkCount = ptr<uint32_t>(c->linkCount);
+  KBEG(TK_CONN_COUNT);
   CK(connectivity_tasks(c->cfg, false, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
                         ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), nullptr, nullptr, 0, c->st,
                         &c->launches));
+  KEND(TK_CONN_COUNT);
   RC(scan_publish(c, mode, linkCount, c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_LINKS,
                   mode == DEVICE ? c->capLinks : NO_CAP));
   uint64_t maxLinks = c->capLinks;
@@ -450,9 +504,11 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
   }
   ENSURE(basis, maxLinks, 4);
   ENSURE(follower, maxLinks, 4);
+  KBEG(TK_CONN_EMIT);
   CK(connectivity_tasks(c->cfg, true, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
                         ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), ptr<uint32_t>(c->basis),
                         ptr<uint32_t>(c->follower), maxLinks, c->st, &c->launches));
+  KEND(TK_CONN_EMIT);
   CK(connectable_streams(ptr<uint32_t>(c->cflags), nTDev, maxT, ptr<uint32_t>(c->connS), ptr<uint32_t>(c->nonConnS),
                          c->st, &c->launches));
   RC(scan_publish(c, mode, ptr<uint32_t>(c->connS), c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_CONN, NO_CAP));
@@ -539,6 +595,11 @@ int begin_run(trax_ctx* c) {
 int run_stage(trax_ctx* c, int stage) {
   if (stage > 1 && c->stage < stage - 1) return fail(c, TRAX_ERR_STATE, "the previous stage has not run");
   int rc = TRAX_OK;
+  if (stage == 1) {
+    for (bool& u : c->stageUsed) u = false;
+    for (bool& u : c->kUsed) u = false;
+  }
+  cudaEventRecord(c->stageEv[stage - 1], c->st);
   switch (stage) {
     case 1: rc = begin_run(c); if (!rc) rc = stage_grid(c, SYNCED); break;
     case 2: rc = stage_pairs(c, SYNCED); break;
@@ -550,20 +611,24 @@ int run_stage(trax_ctx* c, int stage) {
     default: return fail(c, TRAX_ERR_ARG, "unknown stage");
   }
   if (rc) return rc;
+  cudaEventRecord(c->stageEv[stage], c->st);
+  c->stageUsed[stage - 1] = true;
   RC(check_device_error(c));
   c->stage = stage;
   return TRAX_OK;
 }
 
 int chain_device(trax_ctx* c, bool linking) {
-  RC(stage_grid(c, DEVICE));
-  RC(stage_pairs(c, DEVICE));
-  RC(stage_predict(c, DEVICE));
-  RC(stage_filter(c, DEVICE));
-  if (linking) {
-    RC(stage_connectivity(c, DEVICE));
-    RC(stage_fit(c, DEVICE));
-    RC(stage_ca(c, DEVICE));
+  for (bool& u : c->stageUsed) u = false;
+  for (bool& u : c->kUsed) u = false;
+  int (*stages[N_STAGES])(trax_ctx*, Mode) = {stage_grid, stage_pairs, stage_predict, stage_filter,
+                                              stage_connectivity, stage_fit, stage_ca};
+  const int n = linking ? N_STAGES : 4;
+  CK(record(c, c->stageEv[0]));
+  for (int s = 0; s < n; ++s) {
+    RC(stages[s](c, DEVICE));
+    CK(record(c, c->stageEv[s + 1]));
+    c->stageUsed[s] = true;
   }
   return TRAX_OK;
 }
@@ -668,6 +733,8 @@ int trax_create(trax_ctx** out, int device) {
   if (e == cudaSuccess) e = cudaMemset(c->slots.p, 0, sizeof(uint32_t) * 64);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  for (int i = 0; i <= N_STAGES && e == cudaSuccess; ++i) e = cudaEventCreate(&c->stageEv[i]);
+  for (int i = 0; i < 2 * TK_N && e == cudaSuccess; ++i) e = cudaEventCreate(&c->kEv[i]);
   if (e == cudaSuccess) e = grid_prepare(device);
   if (e != cudaSuccess) {
     trax_destroy(c);
@@ -694,6 +761,10 @@ void trax_destroy(trax_ctx* c) {
   if (c->hSlots) cudaFreeHost(c->hSlots);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
+  for (cudaEvent_t& ev : c->stageEv)
+    if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t& ev : c->kEv)
+    if (ev) cudaEventDestroy(ev);
   if (c->st) cudaStreamDestroy(c->st);
   delete c;
 }
@@ -916,6 +987,23 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
     return TRAX_OK;
   }
   return fail(c, TRAX_ERR_CAPACITY, "capacity exceeded after recalibration");
+}
+
+int trax_get_timings(trax_ctx* c, float* stage_ms, float* kernel_ms) {
+  if (!c) return TRAX_ERR_ARG;
+  CK(cudaStreamSynchronize(c->st));
+  for (int s = 0; s < N_STAGES; ++s) {
+    float ms = -1.0f;
+    if (c->stageUsed[s] && cudaEventElapsedTime(&ms, c->stageEv[s], c->stageEv[s + 1]) != cudaSuccess) ms = -1.0f;
+    if (stage_ms) stage_ms[s] = ms;
+  }
+  for (int k = 0; k < TK_N; ++k) {
+    float ms = -1.0f;
+    if (c->kUsed[k] && cudaEventElapsedTime(&ms, c->kEv[2 * k], c->kEv[2 * k + 1]) != cudaSuccess) ms = -1.0f;
+    if (kernel_ms) kernel_ms[k] = ms;
+  }
+  cudaGetLastError();  // clear a "not ready"/"invalid handle" from unused events
+  return TRAX_OK;
 }
 
 int trax_get_stats(trax_ctx* c, trax_batch_stats* s) {
