@@ -143,6 +143,31 @@ int trax_cellular_automaton(trax_ctx* ctx, uint64_t* n_track_entries);
  * the device; single-pass decoupled-lookback scan). */
 int trax_prefix_sum(trax_ctx* ctx, uint32_t* data, uint64_t n);
 
+/* Allocation-free exclusive uint32 scan of n elements from d_in to d_out
+ * (device pointers owned by the caller; in place allowed), on the caller's
+ * `stream` (a cudaStream_t, NULL for the legacy default stream) of the
+ * current device.  No counterpart in the reference: it exists for callers
+ * that must not allocate device memory -- code running inside another
+ * framework's memory pool or under an allocator that forbids new device
+ * allocations (a cudaMalloc there can fail, stall or break a budget), and
+ * code that has to work when device memory is already exhausted.  It calls
+ * no cudaMalloc, no cudaFree and no allocating library routine, and needs no
+ * trax_ctx.
+ *   - Its scratch (tile ticket, error word, one look-back status word per
+ *     2048-element tile) is a fixed array inside the library, present on
+ *     every GPU that loads it until the process exits; n is therefore limited
+ *     to TRAX_NOALLOC_SCAN_MAX elements, larger n returns TRAX_ERR_ARG.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - All calls share the array and each call clears what it uses; calls
+ *     whose work overlaps on the GPU (other streams, other host threads) race.
+ *   - The call waits for its stream to finish, so that a timed-out look-back
+ *     wait is reported (TRAX_ERR_TIMEOUT).
+ * A message is written to err_msg (err_len bytes, may be NULL) on failure. */
+#define TRAX_NOALLOC_SCAN_MAX (16ull * 1024ull * 1024ull)
+int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n, void* stream, char* err_msg,
+                            size_t err_len);
+
 /* ------------------------------------------------------------- batched
  * The whole chain (buildTriplets, TripletBuilder.cpp:312-467) for all
  * uploaded events in one pass of batched launches, optionally replayed from a

@@ -224,3 +224,103 @@ cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint
 }
 
 }  // namespace trax
+
+// ------------------------------------------------------------------------
+// Allocation-free prefix sum for callers that cannot allocate device memory
+// (see trax_prefix_sum_noalloc in include/trax/trax.h).
+//
+// The single-pass scan needs scratch besides its input and output: a tile
+// ticket, an error word and one look-back status word per tile.  Here that
+// scratch is a fixed file-scope device array, so the call itself never
+// allocates.  It is sized for TRAX_NOALLOC_SCAN_MAX elements and, like any
+// __device__ variable, lives on every GPU that loads this library until the
+// process exits.  All calls share it: each call clears the part it uses
+// before its kernel runs, and two calls whose work overlaps on the GPU (on
+// different streams, or from different host threads) race on it.
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/trax/trax.h"
+
+namespace {
+
+constexpr uint64_t NOALLOC_TILES = (TRAX_NOALLOC_SCAN_MAX + trax::SCAN_TILE - 1) / trax::SCAN_TILE;
+constexpr size_t NOALLOC_HEADER = 256;  // ticket at byte 0, error word at byte 4
+constexpr size_t NOALLOC_BYTES = NOALLOC_HEADER + NOALLOC_TILES * sizeof(unsigned long long);
+
+static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+void noalloc_msg(char* buf, size_t len, const char* msg) {
+  if (buf && len) {
+    snprintf(buf, len, "%s", msg);
+  }
+}
+
+}  // namespace
+
+extern "C" int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n, void* stream,
+                                       char* err_msg, size_t err_len) {
+  noalloc_msg(err_msg, err_len, "");
+  if (n == 0) return TRAX_OK;
+  if (!d_in || !d_out) {
+    noalloc_msg(err_msg, err_len, "trax_prefix_sum_noalloc: null device pointer");
+    return TRAX_ERR_ARG;
+  }
+  if (n > TRAX_NOALLOC_SCAN_MAX) {
+    char b[160];
+    snprintf(b, sizeof b, "trax_prefix_sum_noalloc: %llu elements exceed the fixed scratch limit of %llu",
+             (unsigned long long)n, (unsigned long long)TRAX_NOALLOC_SCAN_MAX);
+    noalloc_msg(err_msg, err_len, b);
+    return TRAX_ERR_ARG;
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
+    noalloc_msg(err_msg, err_len, "trax_prefix_sum_noalloc: no usable current device");
+    return TRAX_ERR_CUDA;
+  }
+  void* base = nullptr;
+  {
+    // first call on this device: look up the device address of the array
+    // (host code may not use the symbol itself as a device pointer)
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
+      if (e != cudaSuccess || !p) {
+        noalloc_msg(err_msg, err_len, "trax_prefix_sum_noalloc: cudaGetSymbolAddress failed");
+        return TRAX_ERR_CUDA;
+      }
+      g_noalloc_addr[dev] = p;
+    }
+    base = g_noalloc_addr[dev];
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const uint64_t tiles = (n + trax::SCAN_TILE - 1) / trax::SCAN_TILE;
+  uint32_t* ticket = static_cast<uint32_t*>(base);
+  uint32_t* err = ticket + 1;
+  unsigned long long* status = reinterpret_cast<unsigned long long*>(static_cast<char*>(base) + NOALLOC_HEADER);
+  // the ticket, the error word and the status words of this call start at zero
+  e = cudaMemsetAsync(base, 0, NOALLOC_HEADER + tiles * sizeof(unsigned long long), st);
+  if (e == cudaSuccess) {
+    trax::scan_kernel<<<(unsigned)tiles, trax::SCAN_THREADS, 0, st>>>(d_in, d_out, n, nullptr, 0, status, ticket,
+                                                                      err);
+    e = cudaGetLastError();
+  }
+  uint32_t hostErr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hostErr, err, sizeof(hostErr), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    noalloc_msg(err_msg, err_len, cudaGetErrorString(e));
+    return TRAX_ERR_CUDA;
+  }
+  if (hostErr & TRAX_EBIT_TIMEOUT) {
+    noalloc_msg(err_msg, err_len, "trax_prefix_sum_noalloc: a bounded look-back wait ran out");
+    return TRAX_ERR_TIMEOUT;
+  }
+  return TRAX_OK;
+}
