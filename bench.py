@@ -63,44 +63,6 @@ def parse():
     return p.parse_args()
 
 
-# ------------------------------------------------------------------ ranks
-class Ranks:
-    def __init__(self):
-        self.world = int(os.environ.get("WORLD_SIZE", "1"))
-        self.rank = int(os.environ.get("RANK", "0"))
-        self.local = int(os.environ.get("LOCAL_RANK", "0"))
-        self.pg = None
-        if self.world > 1:
-            import torch.distributed as dist
-            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-            dist.init_process_group("gloo", rank=self.rank, world_size=self.world)
-            self.pg = dist
-
-    def barrier(self):
-        if self.pg:
-            self.pg.barrier()
-
-    def max(self, v: float) -> float:
-        if not self.pg:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64)
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum(self, v: float) -> float:
-        if not self.pg:
-            return v
-        import torch
-        t = torch.tensor([v], dtype=torch.float64)
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
-        return float(t.item())
-
-    def close(self):
-        if self.pg:
-            self.pg.destroy_process_group()
-
-
 # ----------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
@@ -241,7 +203,7 @@ def parity_sample(ctx, batch, n=6):
     return f"{'bit-exact' if ok else 'MISMATCH'} against the CPU oracle on the first {n} events"
 
 
-def run_ours(args, ranks: Ranks):
+def run_ours(args, ranks):
     from trax_gb300 import capi, events
     device = ranks.local
     seed = 2 + 1000 * ranks.rank
@@ -316,7 +278,7 @@ def run_ours(args, ranks: Ranks):
     }
 
     # end to end through the C ABI from host buffers
-    if ranks.rank == 0 or True:
+    if args.e2e_steps > 0:
         e2e_times = []
         bi = int(sum(getattr(batch, k).nbytes for k in ("x", "y", "z", "layer", "det_id", "hit_id", "event"))
                  + batch.event_offsets.nbytes + batch.layer_hits.nbytes + batch.layer_offsets.nbytes)
@@ -349,7 +311,7 @@ def run_ours(args, ranks: Ranks):
     return result
 
 
-def run_reference(args, ranks: Ranks):
+def run_reference(args, ranks):
     if ranks.rank != 0:
         return None
     from oracle import oracle
@@ -387,8 +349,9 @@ def run_reference(args, ranks: Ranks):
 
 
 def main():
+    from trax_gb300.sharding import Ranks
     args = parse()
-    ranks = Ranks()
+    ranks = Ranks("gloo")
     try:
         if args.impl == "reference":
             res = run_reference(args, ranks)

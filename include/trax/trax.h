@@ -129,6 +129,14 @@ int trax_triplet_predict(trax_ctx* ctx, uint64_t* n_candidates);
 /* TripletThetaPhiFilter::run (TripletThetaPhiFilter.h:46-48, .cpp:10-206). */
 int trax_triplet_filter(trax_ctx* ctx, uint64_t* n_triplets);
 
+/* TrackletCollection input for the linking stages: the reference's
+ * TripletConnectivityTight::run takes any HitCollection and TrackletCollection
+ * (TripletConnectivityTight.h:42-44).  The uploaded hits are used as the hit
+ * collection in their input order (no grid build) and h1/h2/h3 index them;
+ * triplets must be grouped by (event, layer triplet), ascending.  Afterwards
+ * trax_connectivity, trax_circle_fit and trax_cellular_automaton can run. */
+int trax_set_tracklets(trax_ctx* ctx, const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, uint64_t n);
+
 /* TripletConnectivityTight::run (TripletConnectivityTight.h:42-44, .cpp:5-475). */
 int trax_connectivity(trax_ctx* ctx, float d_eta_cut, uint64_t* n_links);
 

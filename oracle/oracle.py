@@ -171,6 +171,51 @@ def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1) 
         L.oracle_free(h)
 
 
+class _LinkInput(ctypes.Structure):
+    _fields_ = [("n_hits", ctypes.c_uint32), ("x", ctypes.c_void_p), ("y", ctypes.c_void_p),
+                ("z", ctypes.c_void_p), ("layer", ctypes.c_void_p), ("event", ctypes.c_void_p),
+                ("n_events", ctypes.c_uint32), ("n_lt", ctypes.c_uint32), ("n_triplets", ctypes.c_uint32),
+                ("h1", ctypes.c_void_p), ("h2", ctypes.c_void_p), ("h3", ctypes.c_void_p),
+                ("d_eta_cut", ctypes.c_float)]
+
+
+def link(x, y, z, layer, event, h1, h2, h3, n_events: int, n_lt: int, d_eta_cut: float) -> Dict[str, np.ndarray]:
+    """Connectivity, circle fit and CA on given triplets over hits taken as they are."""
+    L = lib()
+    if not hasattr(L, "_link_ready"):
+        L.oracle_link.argtypes = [ctypes.POINTER(_LinkInput), ctypes.POINTER(ctypes.c_void_p)]
+        L.oracle_link.restype = ctypes.c_int
+        L._link_ready = True
+    keep = []
+
+    def arr(a, dt):
+        a = np.ascontiguousarray(a, dtype=dt)
+        if a.size == 0:
+            a = np.zeros(1, dtype=dt)
+        keep.append(a)
+        return _ptr(a)
+
+    inp = _LinkInput(len(x), arr(x, np.float32), arr(y, np.float32), arr(z, np.float32),
+                     arr(layer, np.uint32), arr(event, np.uint32), n_events, n_lt, len(h1),
+                     arr(h1, np.uint32), arr(h2, np.uint32), arr(h3, np.uint32), d_eta_cut)
+    h = ctypes.c_void_p()
+    if L.oracle_link(ctypes.byref(inp), ctypes.byref(h)) != 0:
+        raise OracleError(L.oracle_last_error().decode())
+    try:
+        d = {}
+        for name in ARRAYS:
+            n = L.oracle_size(h, 0, name.encode())
+            if n < 0:
+                continue
+            dt = np.float32 if name in FLOAT_ARRAYS else np.uint32
+            a = np.zeros(max(n, 1), dtype=dt)
+            L.oracle_copy(h, 0, name.encode(), _ptr(a))
+            d[name] = a[:n]
+        return d
+    finally:
+        L.oracle_free(h)
+
+
 def prefix_sum_blelloch(data: np.ndarray, wg: int) -> np.ndarray:
     a = np.ascontiguousarray(data, dtype=np.uint32).copy()
     lib().oracle_prefix_sum_blelloch(_ptr(a), a.size, wg)

@@ -512,6 +512,8 @@ bool filter_one(const Ctx& c, const PairOut& po, const uint* cand) {
   return valid;
 }
 
+void filter_offsets(const Ctx& c, FilterOut& fo);
+
 // TripletThetaPhiFilter::run (.cpp:10-206): count, popcount, scan, store,
 // offset store and monotonize.
 void filter(const Ctx& c, const PairOut& po, const PredOut& pr, FilterOut& fo) {
@@ -546,7 +548,12 @@ void filter(const Ctx& c, const PairOut& po, const PredOut& pr, FilterOut& fo) {
       pos += valid;
     }
   }
-  // filterOffsetStore (:221-257)
+  filter_offsets(c, fo);
+}
+
+// filterOffsetStore (TripletThetaPhiFilter.h:221-257) + monotonize (:267-280)
+void filter_offsets(const Ctx& c, FilterOut& fo) {
+  const uint nFound = (uint)fo.h1.size();
   fo.offsets.assign((size_t)c.E * c.nLT + 1, 0u);
   for (uint gid = 0; gid < nFound; ++gid) {
     uint hitId = fo.h1[gid];
@@ -878,6 +885,67 @@ std::string run_group(const oracle_input* in, uint e0, uint e1, Group& G) {
   return std::string();
 }
 
+// Connectivity, circle fit and CA on caller-provided triplets over a hit
+// collection taken as is (TripletConnectivityTight::run takes any
+// HitCollection and TrackletCollection, TripletConnectivityTight.h:42-44).
+std::string run_link(const oracle_link_input* in, Group& G) {
+  Ctx c;
+  oracle_input dummy;
+  memset(&dummy, 0, sizeof(dummy));
+  dummy.d_eta_cut = in->d_eta_cut;
+  c.in = &dummy;
+  c.E = in->n_events;
+  c.L = 0;
+  c.nZ = c.nP = c.C = 0;
+  c.nLT = in->n_lt;
+  if (c.E == 0 || c.nLT == 0) return "need at least one event and one layer triplet";
+  Hits& h = c.h;
+  h.x.assign(in->x, in->x + in->n_hits);
+  h.y.assign(in->y, in->y + in->n_hits);
+  h.z.assign(in->z, in->z + in->n_hits);
+  h.layer.assign(in->layer, in->layer + in->n_hits);
+  h.evt.assign(in->event, in->event + in->n_hits);
+  FilterOut fo;
+  fo.h1.assign(in->h1, in->h1 + in->n_triplets);
+  fo.h2.assign(in->h2, in->h2 + in->n_triplets);
+  fo.h3.assign(in->h3, in->h3 + in->n_triplets);
+  for (uint t = 0; t < in->n_triplets; ++t) {
+    if (fo.h1[t] >= in->n_hits || fo.h2[t] >= in->n_hits || fo.h3[t] >= in->n_hits) return "triplet hit out of range";
+    if (h.layer[fo.h1[t]] < 1 || h.layer[fo.h1[t]] > c.nLT || h.evt[fo.h1[t]] >= c.E)
+      return "triplet first hit outside the layer-triplet/event range";
+  }
+  filter_offsets(c, fo);
+  ConnOut co;
+  connectivity(c, fo, co);
+  std::vector<float> pt;
+  CAOut ca;
+  if (!co.noLinks) {
+    circle_fit(c, fo, co, pt);
+    cellular_automaton((uint)fo.h1.size(), co, pt, ca);
+  }
+  G.u("trip_offsets") = fo.offsets;
+  G.put_f("eta", co.eta);
+  G.u("link_basis") = co.basis;
+  G.u("link_follower") = co.follower;
+  G.u("connectable") = co.connectable;
+  G.u("non_connectable") = co.nonConnectable;
+  G.put_f("pt", pt);
+  G.u("ca_states") = ca.states;
+  G.u("ca_best") = ca.best;
+  G.u("tracks") = ca.tracks;
+  G.u("track_offsets") = ca.trackOffsets;
+  std::vector<uint>& st = G.u("stats");
+  st.assign(ST_N, 0u);
+  st[ST_TRIPLETS] = (uint)fo.h1.size();
+  st[ST_LINKS] = (uint)co.basis.size();
+  st[ST_CONNECTABLE] = (uint)co.connectable.size();
+  st[ST_NONCONN] = (uint)co.nonConnectable.size();
+  st[ST_CA_ITER] = ca.iterations;
+  st[ST_TRACK_ENTRIES] = (uint)ca.tracks.size();
+  st[ST_NO_LINKS] = co.noLinks ? 1u : 0u;
+  return std::string();
+}
+
 std::string validate(const oracle_input* in) {
   if (in->n_layers == 0 || in->n_z == 0 || in->n_phi == 0) return "n_layers, n_z and n_phi must be positive";
   uint64_t cells = (uint64_t)(in->n_z + 1) * (in->n_phi + 1);
@@ -959,6 +1027,20 @@ int oracle_run(const oracle_input* in, oracle_result** out) {
       delete r;
       return -2;
     }
+  *out = r;
+  return 0;
+}
+
+int oracle_link(const oracle_link_input* in, oracle_result** out) {
+  *out = nullptr;
+  oracle_result* r = new oracle_result();
+  r->groups.resize(1);
+  std::string err = run_link(in, r->groups[0]);
+  if (!err.empty()) {
+    set_error(err);
+    delete r;
+    return -1;
+  }
   *out = r;
   return 0;
 }

@@ -58,6 +58,26 @@ typedef struct oracle_result oracle_result;
 
 // Runs the whole chain.  Returns 0 on success, a negative code on invalid input.
 int oracle_run(const oracle_input* in, oracle_result** out);
+
+// Connectivity, circle fit and CA on given triplets over a hit collection
+// used as is (one event group).  Triplets must be grouped by (event, layer
+// triplet) in ascending order, layer triplet p starting on layer p+1.
+typedef struct oracle_link_input {
+  uint32_t n_hits;
+  const float* x;
+  const float* y;
+  const float* z;
+  const uint32_t* layer;
+  const uint32_t* event;
+  uint32_t n_events;
+  uint32_t n_lt;
+  uint32_t n_triplets;
+  const uint32_t* h1;
+  const uint32_t* h2;
+  const uint32_t* h3;
+  float d_eta_cut;
+} oracle_link_input;
+int oracle_link(const oracle_link_input* in, oracle_result** out);
 void oracle_free(oracle_result* r);
 const char* oracle_last_error(void);
 

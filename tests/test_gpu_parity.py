@@ -158,3 +158,50 @@ def test_hits_outside_grid_rejected(trax_lib):
         with pytest.raises(trax_lib.TraxError) as e:
             c.grid_build()
         assert e.value.code == 5
+
+
+def _kat_batch():
+    from tests.test_oracle_kats import load_kat
+    kat, cols, t = load_kat()
+    n_layers = int(cols["layer"].max())
+    lh = np.bincount(cols["layer"] - 1, minlength=n_layers).astype(np.uint32).reshape(1, n_layers)
+    w = events.workload(2)
+    lts = [events.LayerTriplet(p + 1, p + 2, p + 3, 0.01, 0.037, 0.05, 0.032, 1.0, 2, 10.0, 2, 4)
+           for p in range(kat["n_layer_triplets"])]
+    proto = events.EventBatch(x=None, y=None, z=None, layer=None, det_id=None, hit_id=None, event=None,
+                              event_offsets=None, layer_hits=None, layer_offsets=None,
+                              min_r=np.asarray(w.radii[:n_layers], np.float32) - 0.1,
+                              max_r=np.asarray(w.radii[:n_layers], np.float32) + 0.1, lts=lts, n_z=20, n_phi=20,
+                              min_pt=1.0, d_eta_cut=kat["d_eta_cut"])
+    cols = dict(cols, det_id=np.zeros_like(cols["layer"]), hit_id=np.zeros_like(cols["layer"]))
+    return kat, events._assemble(cols, lh, proto), t
+
+
+@pytest.mark.parametrize("shuffle", [False, True])
+def test_tight_connectivity_kat_gpu(ctx, oracle_lib, shuffle):
+    # TripletConnectivityTest.h:66-94 through trax_set_tracklets + the linking stages
+    kat, batch, t = _kat_batch()
+    if shuffle:  # unsorted segments: the connectivity scans like the reference
+        rng = np.random.default_rng(3)
+        t = np.concatenate([t[4 * p:4 * p + 4][rng.permutation(4)] for p in range(4)])
+    ref = oracle_lib.link(batch.x, batch.y, batch.z, batch.layer, batch.event, t[:, 0], t[:, 1], t[:, 2], 1,
+                          kat["n_layer_triplets"], kat["d_eta_cut"])
+    ctx.upload(batch)
+    ctx.set_tracklets(t[:, 0], t[:, 1], t[:, 2])
+    assert ctx.connectivity(kat["d_eta_cut"]) == 3
+    ctx.circle_fit()
+    ctx.cellular_automaton()
+    got = ctx.results()
+    compare(got, ref, ["link_basis", "link_follower", "connectable", "non_connectable", "ca_states", "tracks",
+                       "track_offsets", "eta", "pt"])
+    if not shuffle:
+        assert np.stack([got["link_basis"], got["link_follower"]], 1).tolist() == kat["expected"]["links"]
+        assert got["ca_states"].tolist() == kat["expected"]["ca_states"]
+
+
+def test_config0_golden_gpu(ctx):
+    from tests.test_oracle_kats import golden_batch
+    b, d = golden_batch()
+    got = stagewise(ctx, b)
+    for k in ("grid", "perm", "pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "trip_offsets"):
+        assert np.array_equal(got[k], d["oracle_" + k]), k

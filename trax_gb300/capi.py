@@ -23,7 +23,8 @@ ERRORS = {1: "TRAX_ERR_CUDA", 2: "TRAX_ERR_ARG", 3: "TRAX_ERR_CAPACITY", 4: "TRA
 
 EXPORTED = [
     "trax_create", "trax_destroy", "trax_last_error", "trax_version", "trax_set_layer_triplets",
-    "trax_set_geometry", "trax_set_grid", "trax_upload_hits", "trax_grid_build", "trax_pair_gen",
+    "trax_set_geometry", "trax_set_grid", "trax_upload_hits", "trax_grid_build", "trax_set_tracklets",
+    "trax_pair_gen", "trax_prefix_sum_noalloc",
     "trax_triplet_predict", "trax_triplet_filter", "trax_connectivity", "trax_circle_fit",
     "trax_cellular_automaton", "trax_prefix_sum", "trax_seed_batch", "trax_get_stats", "trax_get_pairs",
     "trax_get_timings", "trax_get_candidates", "trax_get_triplets", "trax_get_triplet_eta_pt", "trax_get_links",
@@ -92,6 +93,7 @@ def load() -> ctypes.CDLL:
             "trax_set_grid": ([vp, u32, u32], i32),
             "trax_upload_hits": ([vp, vp, u32, vp, vp, vp, u32, u32], i32),
             "trax_grid_build": ([vp], i32),
+            "trax_set_tracklets": ([vp, vp, vp, vp, u64], i32),
             "trax_pair_gen": ([vp, pu64], i32),
             "trax_triplet_predict": ([vp, pu64], i32),
             "trax_triplet_filter": ([vp, pu64], i32),
@@ -220,6 +222,11 @@ class Context:
     def grid_build(self):
         self._check(self._L.trax_grid_build(self._h))
 
+    def set_tracklets(self, h1: np.ndarray, h2: np.ndarray, h3: np.ndarray):
+        """Caller triplets over the uploaded hits (input order) for the linking stages."""
+        a, b, c = (np.ascontiguousarray(v, dtype=np.uint32) for v in (h1, h2, h3))
+        self._check(self._L.trax_set_tracklets(self._h, _p(a), _p(b), _p(c), a.size))
+
     def _count(self, fn, *args) -> int:
         n = ctypes.c_uint64()
         self._check(fn(self._h, *args, ctypes.byref(n)))
@@ -337,7 +344,10 @@ class Context:
 
     def results(self) -> Dict[str, np.ndarray]:
         """All stage outputs in the oracle's naming."""
-        out = {"perm": self.hit_perm(), "grid": self.grid()}
+        try:
+            out = {"perm": self.hit_perm(), "grid": self.grid()}
+        except TraxError:  # tracklets given directly: no grid was built
+            out = {"perm": self.hit_perm(), "grid": np.zeros(0, np.uint32)}
         p, po = self.pairs()
         out["pairs"], out["pair_offsets"] = p.reshape(-1), po
         c, co = self.candidates()

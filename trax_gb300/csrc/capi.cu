@@ -123,6 +123,10 @@ struct trax_ctx {
   uint64_t pairSent = 0, candSent = 0;
   int stage = 0;  // last completed stage: 1 grid .. 7 CA
   bool noLinks = true;
+  // triplets of every segment ordered by (second hit, first hit): true for the
+  // chain's own filter output; checked for caller-provided triplets
+  bool sortedSegments = true;
+  bool identityHits = false;  // hit collection taken as uploaded (trax_set_tracklets)
   uint32_t launches = 0;
   // DEVICE-mode capacities and the captured graph
   uint64_t capTasks = 0, capPairs = 0, capCands = 0, capT = 0, capLinks = 0, capTracks = 0;
@@ -490,8 +494,8 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
   uint32_t* linkCount = ptr<uint32_t>(c->linkCount);
   KBEG(TK_CONN_COUNT);
   CK(connectivity_tasks(c->cfg, false, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
-                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), nullptr, nullptr, 0, c->st,
-                        &c->launches));
+                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), nullptr, nullptr, 0,
+                        c->sortedSegments, c->st, &c->launches));
   KEND(TK_CONN_COUNT);
   RC(scan_publish(c, mode, linkCount, c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_LINKS,
                   mode == DEVICE ? c->capLinks : NO_CAP));
@@ -507,7 +511,7 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
   KBEG(TK_CONN_EMIT);
   CK(connectivity_tasks(c->cfg, true, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
                         ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), ptr<uint32_t>(c->basis),
-                        ptr<uint32_t>(c->follower), maxLinks, c->st, &c->launches));
+                        ptr<uint32_t>(c->follower), maxLinks, c->sortedSegments, c->st, &c->launches));
   KEND(TK_CONN_EMIT);
   CK(connectable_streams(ptr<uint32_t>(c->cflags), nTDev, maxT, ptr<uint32_t>(c->connS), ptr<uint32_t>(c->nonConnS),
                          c->st, &c->launches));
@@ -587,6 +591,8 @@ int stage_ca(trax_ctx* c, Mode mode) {
 
 int begin_run(trax_ctx* c) {
   RC(build_config(c));
+  c->sortedSegments = true;
+  c->identityHits = false;
   CK(cudaSetDevice(c->device));
   CK(cudaMemsetAsync(c->slots.p, 0, sizeof(uint32_t) * S_N, c->st));
   return TRAX_OK;
@@ -854,6 +860,65 @@ int trax_upload_hits(trax_ctx* c, const trax_hits_soa* h, uint32_t n_hits, const
 
 int trax_grid_build(trax_ctx* c) { return c ? run_stage(c, 1) : TRAX_ERR_ARG; }
 
+int trax_set_tracklets(trax_ctx* c, const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, uint64_t n) {
+  if (!c || (n && (!h1 || !h2 || !h3))) return fail(c, TRAX_ERR_ARG, "null triplet columns");
+  RC(begin_run(c));
+  const Mode mode = SYNCED;
+  const uint64_t nh = c->nHits;
+  if (n > 0xfffffff0ull) return fail(c, TRAX_ERR_ARG, "too many triplets");
+  // host-side validation against the uploaded layer and event columns
+  std::vector<uint32_t> layer(nh), evt(nh);
+  if (nh) {
+    CK(cudaMemcpyAsync(layer.data(), c->in_layer.p, nh * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(evt.data(), c->in_evt.p, nh * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  }
+  uint64_t prevKey = 0;
+  for (uint64_t t = 0; t < n; ++t) {
+    if (h1[t] >= nh || h2[t] >= nh || h3[t] >= nh) return fail(c, TRAX_ERR_ARG, "triplet hit index out of range");
+    const uint32_t l = layer[h1[t]], e = evt[h1[t]];
+    if (l < 1 || l > c->cfg.nLT || e >= c->E)
+      return fail(c, TRAX_ERR_ARG, "a triplet's first hit lies outside the layer-triplet/event range");
+    const uint64_t key = (uint64_t)e * c->cfg.nLT + (l - 1);
+    if (key < prevKey) return fail(c, TRAX_ERR_ARG, "triplets must be grouped by (event, layer triplet)");
+    if (t > 0 && key == prevKey && (h2[t] < h2[t - 1] || (h2[t] == h2[t - 1] && h1[t] < h1[t - 1])))
+      c->sortedSegments = false;  // connectivity then scans like the reference
+    prevKey = key;
+  }
+  ENSURE(px, nh, 4); ENSURE(py, nh, 4); ENSURE(pz, nh, 4);
+  ENSURE(player, nh, 4); ENSURE(pdet, nh, 4); ENSURE(phid, nh, 4); ENSURE(pevt, nh, 4); ENSURE(porig, nh, 4);
+  ENSURE(pxyzp, nh, 16);
+  ENSURE(h1, n, 4);
+  ENSURE(h2, n, 4);
+  ENSURE(h3, n, 4);
+  ENSURE(tripOffsets, (size_t)c->cfg.E * c->cfg.nLT + 1, 4);
+  GridInput in;
+  memset(&in, 0, sizeof(in));
+  in.x = ptr<float>(c->in_x);
+  in.y = ptr<float>(c->in_y);
+  in.z = ptr<float>(c->in_z);
+  in.layer = ptr<uint32_t>(c->in_layer);
+  in.det = ptr<uint32_t>(c->in_det);
+  in.hid = ptr<uint32_t>(c->in_hid);
+  in.evt = ptr<uint32_t>(c->in_evt);
+  CK(identity_hits(in, (uint32_t)nh, dev_hits(c), c->st, &c->launches));
+  if (n) {
+    CK(cudaMemcpyAsync(c->h1.p, h1, n * 4, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->h2.p, h2, n * 4, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->h3.p, h3, n * 4, cudaMemcpyHostToDevice, c->st));
+  }
+  c->hSlots[S_TRIPLETS] = (uint32_t)n;
+  CK(cudaMemcpyAsync(slot(c, S_TRIPLETS), c->hSlots + S_TRIPLETS, 4, cudaMemcpyHostToDevice, c->st));
+  CK(triplet_offsets(c->cfg, dev_hits(c), ptr<uint32_t>(c->h1), slot(c, S_TRIPLETS), n,
+                     ptr<uint32_t>(c->tripOffsets), c->st, &c->launches));
+  c->nPairs = c->nCands = 0;
+  c->nT = n;
+  c->identityHits = true;
+  RC(check_device_error(c));
+  c->stage = 4;
+  return TRAX_OK;
+}
+
 int trax_pair_gen(trax_ctx* c, uint64_t* n_pairs) {
   if (!c) return TRAX_ERR_ARG;
   RC(run_stage(c, 2));
@@ -920,6 +985,8 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
   const bool useGraph = opts ? opts->use_graph != 0 : false;
   if (opts && opts->d_eta_cut > 0.0f) c->dEtaCut = opts->d_eta_cut;
   c->launches = 0;
+  c->identityHits = false;
+  c->sortedSegments = true;
   if (!useGraph) {
     CK(cudaEventRecord(c->ev0, c->st));
     RC(run_synced_chain(c, linking));
@@ -1075,7 +1142,7 @@ int trax_get_tracks(trax_ctx* c, uint32_t* states, uint32_t* tracks, uint32_t* t
 
 int trax_get_grid(trax_ctx* c, uint32_t* grid, uint64_t* n_cells) {
   if (!c) return TRAX_ERR_ARG;
-  if (c->stage < 1) return fail(c, TRAX_ERR_STATE, "grid not built");
+  if (c->stage < 1 || c->identityHits) return fail(c, TRAX_ERR_STATE, "grid not built");
   const uint64_t cells = (uint64_t)c->E * c->L * c->cfg.C;
   if (n_cells) *n_cells = cells;
   RC(copy_out(c, grid, c->grid, cells * 4));

@@ -96,7 +96,7 @@ KERNELS = [
     ("atan", float(np.tan(np.pi / 8)), 6),
     ("asin", 0.5, 6),
     ("atanh", float((np.sqrt(2.0) - 1.0) / (np.sqrt(2.0) + 1.0)), 4),
-    ("asinh", 0.5, 7),
+    ("asinh", 1.0, 12),
 ]
 
 

@@ -121,7 +121,31 @@ __global__ void __launch_bounds__(GRID_THREADS)
   }
 }
 
+// The uploaded hits taken as the hit collection as they are (identity
+// order), for the linking stages run on caller-provided triplets.
+__global__ void identity_hits_kernel(GridInput in, uint32_t n, DevHits out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float x = in.x[i], y = in.y[i], z = in.z[i];
+    out.x[i] = x;
+    out.y[i] = y;
+    out.z[i] = z;
+    out.layer[i] = in.layer[i];
+    out.det[i] = in.det[i];
+    out.hid[i] = in.hid[i];
+    out.evt[i] = in.evt[i];
+    out.orig[i] = i;
+    out.xyzp[i] = make_float4(x, y, z, atan2_(y, x));
+  }
+}
+
 }  // namespace
+
+cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStream_t st, uint32_t* launches) {
+  if (n == 0) return cudaSuccess;
+  identity_hits_kernel<<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(in, n, out);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
 
 cudaError_t grid_prepare(int) {
   return cudaFuncSetAttribute(grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(256)
                 const uint32_t* __restrict__ h1, const uint32_t* __restrict__ h2, const uint32_t* __restrict__ h3,
                 const uint32_t* nTDev, const float* __restrict__ eta, const uint32_t* __restrict__ offsets,
                 const uint32_t* __restrict__ segStart, uint32_t* linkCount, uint32_t* flags, uint32_t* basis,
-                uint32_t* follower, uint32_t capLinks) {
+                uint32_t* follower, uint32_t capLinks, bool sortedSegments) {
   const uint32_t S = cfg.E * cfg.nLT;
   const uint32_t nT = S > 0 ? *nTDev : 0u;
   const float dEtaCut = cfg.dEtaCut;
@@ -119,8 +119,13 @@ __global__ void __launch_bounds__(256)
       const uint32_t lo = max(begin, segStart[k]);
       const uint32_t hi = min(end, segStart[k + 1]);
       const float localEta = eta[t];
-      for (uint32_t i = key_lower_bound(h1, h2, lo, hi, inner, outer); i < hi; ++i) {
-        if (h2[i] != outer || h1[i] != inner) break;
+      // sorted segments: binary search to the (h2, h1) run; otherwise scan
+      // the whole range like the reference (caller-provided triplets)
+      for (uint32_t i = sortedSegments ? key_lower_bound(h1, h2, lo, hi, inner, outer) : lo; i < hi; ++i) {
+        if (h2[i] != outer || h1[i] != inner) {
+          if (sortedSegments) break;
+          continue;
+        }
         const bool test = fabs_(localEta - eta[i]) < dEtaCut;
         if (test) {
           if (EMIT) {
@@ -315,15 +320,15 @@ cudaError_t segment_bounds(const DevConfig& cfg, const uint32_t* seg, const uint
 cudaError_t connectivity_tasks(const DevConfig& cfg, bool emit, DevHits hits, TripletView t, const float* eta,
                                const uint32_t* offsets, const uint32_t* segStart, uint32_t* linkCount,
                                uint32_t* flags, uint32_t* basis, uint32_t* follower, uint64_t capLinks,
-                               cudaStream_t st, uint32_t* launches) {
+                               bool sortedSegments, cudaStream_t st, uint32_t* launches) {
   const int blocks = grid_for(t.maxN + 1, 256);
   const uint32_t cap = capLinks > 0xffffffffull ? 0xffffffffu : (uint32_t)capLinks;
   if (emit)
     conn_kernel<true><<<blocks, 256, 0, st>>>(cfg, hits.evt, hits.layer, t.h1, t.h2, t.h3, t.nDev, eta, offsets,
-                                              segStart, linkCount, flags, basis, follower, cap);
+                                              segStart, linkCount, flags, basis, follower, cap, sortedSegments);
   else
     conn_kernel<false><<<blocks, 256, 0, st>>>(cfg, hits.evt, hits.layer, t.h1, t.h2, t.h3, t.nDev, eta, offsets,
-                                               segStart, linkCount, flags, basis, follower, cap);
+                                               segStart, linkCount, flags, basis, follower, cap, sortedSegments);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

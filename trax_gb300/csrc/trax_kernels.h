@@ -43,6 +43,8 @@ struct GridScratch {
 cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid, DevHits out,
                        GridScratch scratch, uint32_t* err, cudaStream_t st, uint32_t* launches);
 cudaError_t grid_prepare(int device);  // one-time kernel attributes
+// hit collection = uploaded hits in input order (plus the packed xyz-phi array)
+cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStream_t st, uint32_t* launches);
 
 // ----------------------------------------------------------------- pairs
 // Per (event, layer triplet) segment: first outer hit and number of outer hits.
@@ -94,7 +96,7 @@ cudaError_t segment_bounds(const DevConfig& cfg, const uint32_t* seg, const uint
 cudaError_t connectivity_tasks(const DevConfig& cfg, bool emit, DevHits hits, TripletView t, const float* eta,
                                const uint32_t* offsets, const uint32_t* segStart, uint32_t* linkCount,
                                uint32_t* flags, uint32_t* basis, uint32_t* follower, uint64_t capLinks,
-                               cudaStream_t st, uint32_t* launches);
+                               bool sortedSegments, cudaStream_t st, uint32_t* launches);
 // flags[k] for k < n-1 -> (flag, !flag) streams for the two compactions; element n-1 and the +1 slot are 0
 cudaError_t connectable_streams(const uint32_t* flags, const uint32_t* nTDev, uint64_t maxT, uint32_t* conn,
                                 uint32_t* nonConn, cudaStream_t st, uint32_t* launches);

@@ -24,7 +24,7 @@
 //            identity acos(x) = 2 asin(sqrt((1-x)/2)) (and pi minus it for x<0).
 //   log    : x = 2^k m, m in [sqrt(1/2), sqrt(2)), log m = 2 atanh(s),
 //            s = (m-1)/(m+1).
-//   asinh  : odd polynomial for |x| <= 1/2, log(|x| + sqrt(x^2+1)) above,
+//   asinh  : odd polynomial for |x| <= 1, log(|x| + sqrt(x^2+1)) above,
 //            log(2|x|) for |x| > 2^12.
 // Multi-part constants (pi = PI_HI + PI_LO) keep the final additions within
 // about one ulp.  Accuracy is tested against float64 (tests/test_math.py) and
@@ -186,7 +186,7 @@ TRAX_HD float atanh_kernel(float t) {  // |t| <= (sqrt2-1)/(sqrt2+1)
   return odd_series(c, t);
 }
 
-TRAX_HD float asinh_kernel(float t) {  // |t| <= 1/2
+TRAX_HD float asinh_kernel(float t) {  // |t| <= 1
   const float c[TRAX_ASINH_NCOEF] = TRAX_ASINH_COEFS;
   return odd_series(c, t);
 }
@@ -301,7 +301,7 @@ TRAX_HD float asinh_(float x) {
   float r;
   if (a < 2.44140625e-04f) {  // 2^-12: asinh(x) = x to within 2^-25 relative
     return x;
-  } else if (a <= 0.5f) {
+  } else if (a <= 1.0f) {
     r = asinh_kernel(a);
   } else if (a > 4096.0f) {
     r = log_(a) + 6.93147180559945309e-01f;

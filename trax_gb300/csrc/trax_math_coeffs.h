@@ -17,6 +17,6 @@
 #define TRAX_ATANH_NCOEF 5
 #define TRAX_ATANH_COEFS { 3.333333433e-01f, 1.999999732e-01f, 1.428605467e-01f, 1.108811945e-01f, 9.791719168e-02f }
 
-// asinh: t in [0, 0.5], max rel err 1.02 x 2^-24
-#define TRAX_ASINH_NCOEF 8
-#define TRAX_ASINH_COEFS { -1.666666716e-01f, 7.499999553e-02f, -4.464256391e-02f, 3.037548624e-02f, -2.229249477e-02f, 1.676933840e-02f, -1.139061060e-02f, 4.860905930e-03f }
+// asinh: t in [0, 1], max rel err 1.10 x 2^-24
+#define TRAX_ASINH_NCOEF 13
+#define TRAX_ASINH_COEFS { -1.666666716e-01f, 7.499999553e-02f, -4.464269429e-02f, 3.037952445e-02f, -2.235094644e-02f, 1.723148860e-02f, -1.348629035e-02f, 1.019633468e-02f, -6.920428015e-03f, 3.852281952e-03f, -1.582941040e-03f, 4.152705369e-04f, -5.134236926e-05f }
