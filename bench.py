@@ -60,6 +60,7 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-parity", action="store_true")
+    p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: the workload's)")
     return p.parse_args()
 
 
@@ -162,7 +163,9 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells):
 
 
 def chain_bytes(st, n_hits, cells, n_layers):
-    # SURVEY-style per-batch algorithmic bytes of the whole chain
+    # per-batch algorithmic bytes of the whole chain: hits read and written by
+    # the grid build, every intermediate array written once and read once,
+    # the CA's per-level link and state traffic
     P, Cc, T, Lk = st.n_pairs, st.n_candidates, st.n_triplets, st.n_links
     return (56 * n_hits + 4 * cells + 16 * P + 16 * Cc + 24 * T + 4 * T + 16 * Lk + 8 * st.n_connectable
             + (8 * Lk + 8 * T) * max(1, n_layers))
@@ -208,6 +211,8 @@ def run_ours(args, ranks):
     device = ranks.local
     seed = 2 + 1000 * ranks.rank
     batch = events.generate(CONFIG, n_events=args.events, seed=seed)
+    if args.grid:
+        batch.n_z, batch.n_phi = (int(v) for v in args.grid.lower().split("x"))
     n_hits = batch.n_hits
     cells = batch.n_events * batch.n_layers * (batch.n_z + 1) * (batch.n_phi + 1)
     ctx = capi.Context(device)

@@ -111,7 +111,7 @@ struct trax_ctx {
   // pair stage
   DevBuf segOuter, taskBase, taskCount, pairs, pairOffsets;
   // prediction / filter
-  DevBuf candCount, cands, candOffsets, flags, h1, h2, h3, tripOffsets;
+  DevBuf candCount, predKeep, cands, candOffsets, flags, h1, h2, h3, tripOffsets;
   // connectivity / fit / CA
   DevBuf eta, segOf, segStart, linkCount, cflags, basis, follower, connS, nonConnS, connIdx, nonConnIdx, pt;
   DevBuf states, inStart, inCursor, inList, best, isBest, handlers, tracks;
@@ -277,9 +277,12 @@ int build_config(trax_ctx* c) {
     g.pairSigmaPhi[p] = sp;
   }
   if (c->minR.size() < c->L) return fail(c, TRAX_ERR_ARG, "geometry has fewer layers than the hits");
+  const float twoR = 2 * g.minRcurv;
   for (uint32_t l = 0; l < c->L; ++l) {
     g.minR[l] = c->minR[l];
     g.maxR[l] = c->maxR[l];
+    g.acosMinR[l] = trax::acos_(trax::div_(g.minR[l], twoR));
+    g.acosMaxR[l] = trax::acos_(trax::div_(g.maxR[l], twoR));
   }
   return TRAX_OK;
 }
@@ -407,11 +410,13 @@ int stage_predict(trax_ctx* c, Mode mode) {
   const uint32_t* nPairsDev = slot(c, S_PAIRS);
   const uint64_t maxPairs = mode == SYNCED ? c->nPairs : c->capPairs;
   ENSURE(candCount, maxPairs + 1, 4);
+  ENSURE(predKeep, maxPairs * TRAX_PRED_KEEP, 4);
   ENSURE(candOffsets, S + 1, 4);
   uint32_t* candCount = ptr<uint32_t>(c->candCount);
   KBEG(TK_PRED_COUNT);
   CK(predict_pairs(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
-                   candCount, nullptr, 0, slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+                   candCount, ptr<uint32_t>(c->predKeep), nullptr, 0, slot(c, S_CAND_SENT), dev_err(c), c->st,
+                   &c->launches));
   KEND(TK_PRED_COUNT);
   RC(scan_publish(c, mode, candCount, c->nPairs, mode == DEVICE ? nPairsDev : nullptr, maxPairs, S_CANDS,
                   mode == DEVICE ? c->capCands : NO_CAP));
@@ -423,7 +428,8 @@ int stage_predict(trax_ctx* c, Mode mode) {
   ENSURE(cands, maxCands, 8);
   KBEG(TK_PRED_EMIT);
   CK(predict_pairs(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
-                   candCount, ptr<uint2>(c->cands), maxCands, slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+                   candCount, ptr<uint32_t>(c->predKeep), ptr<uint2>(c->cands), maxCands, slot(c, S_CAND_SENT),
+                   dev_err(c), c->st, &c->launches));
   KEND(TK_PRED_EMIT);
   CK(predict_offsets(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs, candCount,
                      ptr<uint32_t>(c->candOffsets), c->st, &c->launches));
@@ -654,6 +660,7 @@ int size_device_buffers(trax_ctx* c) {
   ENSURE(taskCount, c->capTasks + 1, 4);
   ENSURE(pairs, c->capPairs, 8);
   ENSURE(candCount, c->capPairs + 1, 4);
+  ENSURE(predKeep, c->capPairs * TRAX_PRED_KEEP, 4);
   ENSURE(cands, c->capCands, 8);
   ENSURE(flags, c->capCands + 1, 4);
   ENSURE(h1, c->capT, 4); ENSURE(h2, c->capT, 4); ENSURE(h3, c->capT, 4);
@@ -758,7 +765,7 @@ void trax_destroy(trax_ctx* c) {
   DevBuf* bufs[] = {&c->in_x, &c->in_y, &c->in_z, &c->in_layer, &c->in_det, &c->in_hid, &c->in_evt, &c->evOff,
                     &c->layHits, &c->layOff, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
-                    &c->segOuter, &c->taskBase, &c->taskCount, &c->pairs, &c->pairOffsets, &c->candCount, &c->cands,
+                    &c->segOuter, &c->taskBase, &c->taskCount, &c->pairs, &c->pairOffsets, &c->candCount, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flags, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,

@@ -60,8 +60,9 @@ __device__ __forceinline__ PairWindow pair_window(const DevConfig& cfg, uint32_t
   w.zLowSector = (uint32_t)max(f2i_sat(floor_(div_(zLow - cfg.minZ, cfg.sZ))), 0);
   w.zHighSector = min(f2u_sat(floor_(div_(zHigh - cfg.minZ, cfg.sZ))) + 1u, cfg.nZ);
   const float twoR = 2 * cfg.minRcurv;
-  tmp = fabs_(acos_(div_(r, twoR)) - acos_(div_(maxR1, twoR)));
-  float dPhi = fabs_(acos_(div_(r, twoR)) - acos_(div_(minR1, twoR)));
+  const float aR = acos_(div_(r, twoR));
+  tmp = fabs_(aR - cfg.acosMaxR[layer]);
+  float dPhi = fabs_(aR - cfg.acosMinR[layer]);
   dPhi = (float)(tmp < dPhi) * dPhi + (float)(tmp > dPhi) * tmp;
   tmp = div_(atan_(tip * (r - minR1)), r * minR1);
   float phiHigh = div_(atan_(tip * (r - maxR1)), r * maxR1);
@@ -163,7 +164,6 @@ __global__ void __launch_bounds__(PAIR_THREADS)
         for (uint32_t j = a2; j < b2; ++j) nFound += pair_valid(w, hits[j]);
       }
       taskCount[k] = nFound;
-      if (k == 0) taskCount[nTasks] = 0u;
     } else {
       const uint32_t pos0 = taskCount[k];
       uint32_t limit = taskCount[k + 1] - pos0;
@@ -235,6 +235,7 @@ __global__ void __launch_bounds__(PAIR_THREADS)
       }
     }
   }
+  if (!EMIT && blockIdx.x == 0 && threadIdx.x == 0) taskCount[nTasks] = 0u;  // the scan's +1 slot
 }
 
 __global__ void pair_offsets_kernel(DevConfig cfg, const uint32_t* taskBase, const uint32_t* pairStart,
@@ -267,8 +268,8 @@ cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, De
                        uint2* pairs, uint64_t capPairs, uint32_t* sentinels, uint32_t* err, cudaStream_t st,
                        uint32_t* launches) {
   const uint32_t cap = capPairs > 0xffffffffull ? 0xffffffffu : (uint32_t)capPairs;
-  if (maxTasks == 0) return cudaSuccess;
-  const int blocks = grid_for(maxTasks, PAIR_THREADS);
+  if (emit && maxTasks == 0) return cudaSuccess;
+  const int blocks = grid_for(maxTasks + 1, PAIR_THREADS);
   if (emit)
     pair_kernel<true><<<blocks, PAIR_THREADS, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
                                                        taskCount, pairs, cap, sentinels, err);

@@ -10,6 +10,7 @@
 // missing predecessor as zero and finishes, so a lost tile can never hang
 // the GPU.
 #include "trax_kernels.h"
+#include "trax_lookback.cuh"
 
 namespace trax {
 
@@ -18,19 +19,6 @@ namespace {
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
 constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-
-constexpr unsigned long long FLAG_AGG = 1ull << 62;
-constexpr unsigned long long FLAG_PREFIX = 2ull << 62;
-
-__device__ __forceinline__ unsigned long long ld_status(const unsigned long long* p) {
-  unsigned long long v;
-  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-  return v;
-}
-
-__device__ __forceinline__ void st_status(unsigned long long* p, unsigned long long v) {
-  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
 
 __global__ void __launch_bounds__(SCAN_THREADS)
     scan_kernel(const uint32_t* __restrict__ in, uint32_t* out, uint64_t nHost, const uint32_t* nDev,
@@ -82,46 +70,8 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     }
     if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
     uint32_t agg = __shfl_sync(0xffffffffu, wi, SCAN_THREADS / 32 - 1);
-    // publish and look back
-    uint32_t excl = 0;
-    if (tile == 0) {
-      if (lane == 0) st_status(&status[0], FLAG_PREFIX | agg);
-    } else {
-      if (lane == 0) st_status(&status[tile], FLAG_AGG | agg);
-      int64_t pred = (int64_t)tile - 1;
-      uint32_t spins = 0;
-      while (true) {
-        int64_t idx = pred - (int64_t)lane;
-        unsigned long long s = (idx >= 0) ? ld_status(&status[idx]) : (FLAG_PREFIX | 0ull);
-        unsigned long long flag = s & (3ull << 62);
-        if (__any_sync(0xffffffffu, flag == 0ull)) {
-          if (++spins < TRAX_SPIN_LIMIT) {
-            __nanosleep(64);
-            continue;
-          }
-          // bounded wait ran out: record it and treat the missing tiles as empty
-          if (lane == 0) raise_error(err, TRAX_EBIT_TIMEOUT);
-          if (flag == 0ull) s = FLAG_AGG;
-          flag = s & (3ull << 62);
-        }
-        uint32_t val = (uint32_t)(s & 0xffffffffull);
-        uint32_t pmask = __ballot_sync(0xffffffffu, flag == FLAG_PREFIX);
-        if (pmask) {
-          uint32_t first = __ffs(pmask) - 1;
-          uint32_t contrib = (lane <= first) ? val : 0u;
-#pragma unroll
-          for (int d = 16; d > 0; d >>= 1) contrib += __shfl_down_sync(0xffffffffu, contrib, d);
-          excl += __shfl_sync(0xffffffffu, contrib, 0);
-          break;
-        }
-        uint32_t contrib = val;
-#pragma unroll
-        for (int d = 16; d > 0; d >>= 1) contrib += __shfl_down_sync(0xffffffffu, contrib, d);
-        excl += __shfl_sync(0xffffffffu, contrib, 0);
-        pred -= 32;
-      }
-      if (lane == 0) st_status(&status[tile], FLAG_PREFIX | (uint32_t)(excl + agg));
-    }
+    // publish and look back (bounded waits)
+    const uint32_t excl = lb_exclusive_prefix(status, tile, agg, err);
     if (lane == 0) s_prefix = excl;
   }
   __syncthreads();

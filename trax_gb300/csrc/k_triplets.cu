@@ -13,6 +13,7 @@
 // .cpp:10-206): a flag per candidate, a scan of the flags and a stable
 // scatter of (h1, h2, h3) keep the candidate order of the reference.
 #include "trax_kernels.h"
+#include "trax_stages.cuh"
 
 namespace trax {
 
@@ -28,110 +29,107 @@ int grid_for(uint64_t items, int threads) {
   return (int)blocks;
 }
 
-template <bool STORE>
+// Count pass (predictCount, :190-219) that also captures the first
+// min(count, TRAX_PRED_KEEP) candidates the store pass would write (the store
+// variant's valid hits, capped at the count; slots it would leave unwritten
+// get the sentinel), so that the store pass is a copy for most pairs.
 __global__ void __launch_bounds__(PRED_THREADS)
-    predict_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
-                   const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
-                   const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev, uint32_t* candCount,
-                   uint2* cands, uint32_t capCands, uint32_t* sentinels) {
+    predict_count_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
+                         const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
+                         const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev, uint32_t* candCount,
+                         uint32_t* keep) {
   const uint32_t nPairs = *nPairsDev;
-  const uint32_t C = cfg.C, nP = cfg.nP;
   for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < nPairs; gid += gridDim.x * blockDim.x) {
     const uint2 pr = pairs[gid];
-    uint32_t pos = 0, limit = 0;
-    uint2* out = nullptr;
-    if (STORE) {
-      pos = candCount[gid];
-      limit = candCount[gid + 1] - pos;
-      if (pos >= capCands) limit = 0;
-      else if (limit > capCands - pos) limit = capCands - pos;
-      out = cands + pos;
-    }
-    uint32_t nFound = 0;
+    uint32_t count = 0;
     if (pr.x != TRAX_SENTINEL) {
-      const uint32_t firstHit = pr.x, secondHit = pr.y;
-      const uint32_t event = hitEvt[firstHit];
-      const uint32_t layerTriplet = hitLayer[firstHit] - 1;  // Q7
-      const uint32_t layer = cfg.layer3[layerTriplet] - 1;
-      const uint32_t* lGrid3 = grid + ((size_t)event * cfg.L + layer) * C;
-      const float sigmaZ = cfg.sigmaZ[layerTriplet];
-      const float sigmaPhi = cfg.sigmaPhi[layerTriplet];
-      const float minLayerRadius = cfg.minR[layer];
-      const float maxLayerRadius = cfg.maxR[layer];
-      const float4 h1 = hits[firstHit], h2 = hits[secondHit];
-      const float p1x = h1.x, p1y = h1.y, p1z = h1.z;
-      const float p2x = h2.x, p2y = h2.y, p2z = h2.z;
-      float tip2 = p1y * (p2x - p1x) - p1x * (p2y - p1y);
-      tip2 *= tip2;
-      tip2 = div_(tip2, (p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
-      float rOrigin;
-      if (!STORE) {
-        rOrigin = p1x * p1x + p1y * p1y;
-        rOrigin = sqrt_(rOrigin - tip2);
-      } else {
-        rOrigin = sqrt_(p1x * p1x + p1y * p1y);
-        rOrigin = sqrt_(rOrigin * rOrigin - tip2);
-      }
-      const float cotTheta = div_(p2z - p1z, sqrt_(p2x * p2x + p2y * p2y - tip2) - rOrigin);
-      float tmp = p1z + (sqrt_(maxLayerRadius * maxLayerRadius - tip2) - rOrigin) * cotTheta;
-      float zLow = p1z + (sqrt_(minLayerRadius * minLayerRadius - tip2) - rOrigin) * cotTheta;
-      float zHigh = (float)(tmp > zLow) * tmp + (float)(tmp < zLow) * zLow;
-      zLow = (float)(tmp > zLow) * zLow + (float)(tmp < zLow) * tmp;
-      zLow -= sigmaZ;
-      zHigh += sigmaZ;
-      const uint32_t zLowSector = (uint32_t)max(f2i_sat(floor_(div_(zLow - cfg.minZ, cfg.sZ))), 0);
-      const uint32_t zHighSector = min(f2u_sat(floor_(div_(zHigh - cfg.minZ, cfg.sZ))) + 1u, cfg.nZ);
-      const float phi = h2.w;  // atan2(p2.y, p2.x)
-      tmp = h1.w;              // atan2(p1.y, p1.x)
-      float dPhi = phi - tmp;
-      dPhi += (dPhi > TRAX_PI_F) ? -2 * TRAX_PI_F : (dPhi < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
-      dPhi = fabs_(dPhi);
-      const float dHits = sqrt_((p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
-      const float twoR = 2 * cfg.minRcurv;
-      tmp = fabs_(acos_(div_(dHits, twoR)) - acos_(div_(maxLayerRadius, twoR)));
-      float phiLow = fabs_(acos_(div_(dHits, twoR)) - acos_(div_(minLayerRadius, twoR)));
-      dPhi = cl_max(dPhi, cl_max(tmp, phiLow));
-      float phiHigh = phi + dPhi + sigmaPhi;
-      phiLow = phi - dPhi - sigmaPhi;
-      const bool wrapAround = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
-      phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
-      phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
-      phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
-      phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
-      const uint32_t phiLowSector = f2u_sat(floor_(div_(phiLow - cfg.minPhi, cfg.sP)));
-      const uint32_t phiHighSector = min(f2u_sat(floor_(div_(phiHigh - cfg.minPhi, cfg.sP))) + 1u, nP);
-      const uint32_t w = wrapAround ? 1u : 0u;
-      for (uint32_t zs = zLowSector; zs < zHighSector; ++zs) {
-        const uint32_t row = zs * (nP + 1);
-        const uint32_t zSectorStart = cell_at(lGrid3, row, C);
-        const uint32_t zSectorEnd = cell_at(lGrid3, row + nP + 1, C);  // Q8
-        const uint32_t len = zSectorEnd - zSectorStart;
-        const uint32_t end2 = w * zSectorEnd + cell_at(lGrid3, row + phiHighSector, C) - w * zSectorStart;
-        for (uint32_t j = cell_at(lGrid3, row + phiLowSector, C); j < end2; ++j) {
-          const uint32_t index = j - (uint32_t)(j >= zSectorEnd) * len;
-          const float4 h = hits[index];
-          bool valid = zLow <= h.z && h.z <= zHigh;
-          const float actPhi = h.w;
-          valid = valid && ((!wrapAround && (phiLow <= actPhi && actPhi <= phiHigh)) ||
-                            (wrapAround && ((phiLow <= actPhi && actPhi <= TRAX_PI_F) ||
-                                            (-TRAX_PI_F <= actPhi && actPhi <= phiHigh))));
-          if (STORE && valid) {
-            if (nFound < limit) out[nFound] = make_uint2(gid, index);
+      const uint32_t event = hitEvt[pr.x];
+      const uint32_t lt = hitLayer[pr.x] - 1;  // Q7
+      const uint32_t layer = cfg.layer3[lt] - 1;
+      const uint32_t* lG3 = grid + ((size_t)event * cfg.L + layer) * cfg.C;
+      const PredWindow w = pred_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
+      // One walk over the union of both variants' z rows: the phi test is
+      // common, the z test and the row range differ.  Each variant's valid
+      // hits come out in its own visit order.
+      const uint32_t C = cfg.C, nP = cfg.nP;
+      uint32_t* slot = keep + (size_t)gid * TRAX_PRED_KEEP;
+      uint32_t nStore = 0;
+      const uint32_t zLo = min(w.zLoSec[0], w.zLoSec[1]), zHi = max(w.zHiSec[0], w.zHiSec[1]);
+      for (uint32_t zs = zLo; zs < zHi; ++zs) {
+        const bool in0 = zs >= w.zLoSec[0] && zs < w.zHiSec[0];
+        const bool in1 = zs >= w.zLoSec[1] && zs < w.zHiSec[1];
+        uint32_t a[2], b[2];
+        pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
+#pragma unroll
+        for (int part = 0; part < 2; ++part) {
+          for (uint32_t j = a[part]; j < b[part]; ++j) {
+            const float4 h = hits[j];
+            if (!pred_phi_ok(w, h.w)) continue;
+            count += (in0 && w.zLow[0] <= h.z && h.z <= w.zHigh[0]);
+            if (in1 && w.zLow[1] <= h.z && h.z <= w.zHigh[1]) {
+              if (nStore < TRAX_PRED_KEEP) slot[nStore] = j;
+              ++nStore;
+            }
           }
-          nFound += valid;
-          if (STORE && nFound >= limit) break;  // pos < nextThread (:376-377)
         }
-        if (STORE && nFound >= limit) break;
       }
+      // the store pass writes at most `count` candidates; missing ones are
+      // slots the reference leaves unwritten
+      const uint32_t k = min(count, (uint32_t)TRAX_PRED_KEEP);
+      for (uint32_t q = nStore; q < k; ++q) slot[q] = TRAX_SENTINEL;
     }
-    if (!STORE) {
-      candCount[gid] = nFound;
-      if (gid == 0) candCount[nPairs] = 0u;
-    } else if (nFound < limit) {
-      atomicAdd(sentinels, limit - nFound);
-      for (uint32_t q = nFound; q < limit; ++q) out[q] = make_uint2(gid, TRAX_SENTINEL);
-    }
+    candCount[gid] = count;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) candCount[nPairs] = 0u;  // the scan's +1 slot
+}
+
+// Store pass (predictStore, :358-402): candidates (pair, hit3) at the
+// scanned position; copied from the captured slots, re-walked only when a
+// pair has more candidates than slots.
+__global__ void __launch_bounds__(PRED_THREADS)
+    predict_store_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
+                         const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
+                         const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev,
+                         const uint32_t* __restrict__ candStart, const uint32_t* __restrict__ keep, uint2* cands,
+                         uint32_t capCands, uint32_t* sentinels) {
+  const uint32_t nPairs = *nPairsDev;
+  uint32_t sent = 0;
+  for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < nPairs; gid += gridDim.x * blockDim.x) {
+    const uint32_t pos = candStart[gid];
+    uint32_t limit = candStart[gid + 1] - pos;
+    if (pos >= capCands) limit = 0;
+    else if (limit > capCands - pos) limit = capCands - pos;
+    if (limit == 0) continue;
+    uint2* out = cands + pos;
+    if (limit <= (uint32_t)TRAX_PRED_KEEP) {
+      const uint32_t* slot = keep + (size_t)gid * TRAX_PRED_KEEP;
+      for (uint32_t q = 0; q < limit; ++q) {
+        const uint32_t h = slot[q];
+        sent += h == TRAX_SENTINEL;
+        out[q] = make_uint2(gid, h);
+      }
+      continue;
+    }
+    const uint2 pr = pairs[gid];
+    const uint32_t event = hitEvt[pr.x];
+    const uint32_t lt = hitLayer[pr.x] - 1;
+    const uint32_t layer = cfg.layer3[lt] - 1;
+    const uint32_t* lG3 = grid + ((size_t)event * cfg.L + layer) * cfg.C;
+    const PredWindow w = pred_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
+    uint32_t n = 0;
+    const uint32_t C = cfg.C, nP = cfg.nP;
+    for (uint32_t zs = w.zLoSec[1]; zs < w.zHiSec[1] && n < limit; ++zs) {
+      uint32_t a[2], b[2];
+      pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
+      for (int part = 0; part < 2 && n < limit; ++part)
+        for (uint32_t j = a[part]; j < b[part] && n < limit; ++j)
+          if (pred_valid(w, 1, hits[j])) out[n++] = make_uint2(gid, j);
+    }
+    sent += limit - n;
+    for (; n < limit; ++n) out[n] = make_uint2(gid, TRAX_SENTINEL);
+  }
+  for (int d = 16; d > 0; d >>= 1) sent += __shfl_down_sync(0xffffffffu, sent, d);
+  if ((threadIdx.x & 31u) == 0 && sent) atomicAdd(sentinels, sent);
 }
 
 // tripletOffsets of predictStore (:404-418); monotonized afterwards
@@ -159,43 +157,11 @@ __global__ void predict_offsets_kernel(DevConfig cfg, const uint32_t* __restrict
 // filterCount (TripletThetaPhiFilter.h:65-154) for one candidate
 __device__ __forceinline__ bool filter_one(const DevConfig& cfg, const float4* hits, const uint32_t* hitLayer,
                                            const uint2* pairs, uint2 cand) {
-  const uint32_t thirdHit = cand.y;
-  if (thirdHit == TRAX_SENTINEL) return false;
+  if (cand.y == TRAX_SENTINEL) return false;  // a slot the reference never wrote
   const uint2 pr = pairs[cand.x];
-  const uint32_t firstHit = pr.x, secondHit = pr.y;
-  const uint32_t layerTriplet = hitLayer[firstHit] - 1;
-  const float dThetaCut = cfg.dThetaCut[layerTriplet];
-  const float dPhiCut = cfg.dPhiCut[layerTriplet];
-  const float tipCut = cfg.tipCut[layerTriplet];
-  const float4 A = hits[firstHit], B = hits[secondHit], Cc = hits[thirdHit];
-  bool valid = true;
-  float angle1 = atan2_(sqrt_((B.x - A.x) * (B.x - A.x) + (B.y - A.y) * (B.y - A.y)), (B.z - A.z));
-  float angle2 = atan2_(sqrt_((Cc.x - B.x) * (Cc.x - B.x) + (Cc.y - B.y) * (Cc.y - B.y)), (Cc.z - B.z));
-  float delta = fabs_(div_(angle2, angle1));
-  valid = valid && (1 - dThetaCut <= delta && delta <= 1 + dThetaCut);
-  angle1 = atan2_((B.y - A.y), (B.x - A.x));
-  angle2 = atan2_((Cc.y - B.y), (Cc.x - B.x));
-  delta = angle2 - angle1;
-  delta += (delta > TRAX_PI_F) ? -2 * TRAX_PI_F : (delta < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
-  valid = valid && (fabs_(delta) <= dPhiCut);
-  f3 pP1 = make_f3(A.x, A.y, A.x * A.x + A.y * A.y);
-  f3 pP2 = make_f3(B.x, B.y, B.x * B.x + B.y * B.y);
-  f3 pP3 = make_f3(Cc.x, Cc.y, Cc.x * Cc.x + Cc.y * Cc.y);
-  f3 a = sub3(pP2, pP1);
-  f3 b = sub3(pP3, pP1);
-  f3 n = normalize3(cross3(a, b));
-  const float cOx = div_(-n.x, 2 * n.z);
-  const float cOy = div_(-n.y, 2 * n.z);
-  const float cc = -(n.x * pP1.x + n.y * pP1.y + n.z * pP1.z);
-  const float cR = sqrt_(div_(1 - n.z * n.z - 4 * cc * n.z, 4 * n.z * n.z));
-  float vx = -cOx, vy = -cOy;
-  normalize2(vx, vy);
-  const float pCAx = cOx + cR * vx;
-  const float pCAy = cOy + cR * vy;
-  const float tip_squared = pCAx * pCAx + pCAy * pCAy;
-  valid = valid && (tip_squared <= (tipCut * tipCut));
-  valid = valid && (cR >= cfg.minRcurv);
-  return valid;
+  const float4 A = hits[pr.x], B = hits[pr.y];
+  const FilterPair f = filter_prep(cfg, hitLayer[pr.x] - 1, A, B);
+  return filter_cand(cfg, f, B, hits[cand.y]);
 }
 
 __global__ void __launch_bounds__(256)
@@ -247,19 +213,20 @@ __global__ void triplet_offsets_kernel(DevConfig cfg, const uint32_t* __restrict
 }  // namespace
 
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
-                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint2* cands,
-                          uint64_t capCands, uint32_t* sentinels, uint32_t* err, cudaStream_t st,
+                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* keep,
+                          uint2* cands, uint64_t capCands, uint32_t* sentinels, uint32_t* err, cudaStream_t st,
                           uint32_t* launches) {
   (void)err;
-  if (maxPairs == 0) return cudaSuccess;
   const uint32_t cap = capCands > 0xffffffffull ? 0xffffffffu : (uint32_t)capCands;
-  const int blocks = grid_for(maxPairs, PRED_THREADS);
-  if (emit)
-    predict_kernel<true><<<blocks, PRED_THREADS, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                          nPairsDev, candCount, cands, cap, sentinels);
-  else
-    predict_kernel<false><<<blocks, PRED_THREADS, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                           nPairsDev, candCount, cands, cap, sentinels);
+  const int blocks = grid_for(maxPairs + 1, PRED_THREADS);
+  if (emit) {
+    if (maxPairs == 0) return cudaSuccess;
+    predict_store_kernel<<<blocks, PRED_THREADS, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+                                                          nPairsDev, candCount, keep, cands, cap, sentinels);
+  } else {
+    predict_count_kernel<<<blocks, PRED_THREADS, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+                                                          nPairsDev, candCount, keep);
+  }
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

@@ -29,6 +29,9 @@ struct DevConfig {
   float sigmaPhi[TRAX_MAX_LT], tipCut[TRAX_MAX_LT], z0[TRAX_MAX_LT];
   float pairSigmaPhi[TRAX_MAX_LT];  // pairSpreadPhi bit pattern read as float
   float minR[TRAX_MAX_LAYERS], maxR[TRAX_MAX_LAYERS];
+  // acos(r / (2 minRadiusCurvature)) of each layer's min/max radius, computed on
+  // the host with the same trax_math.h code as the kernels would
+  float acosMinR[TRAX_MAX_LAYERS], acosMaxR[TRAX_MAX_LAYERS];
 };
 
 // Grid-ordered hit collection (the reference's HitCollection after GridBuilder).

@@ -61,9 +61,13 @@ cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const u
                          uint32_t* pairOffsets, cudaStream_t st, uint32_t* launches);
 
 // ------------------------------------------------------------ prediction
+// Count pass (emit == false): candCount[nPairs+1] (+1 slot zeroed) and up to
+// TRAX_PRED_KEEP captured candidates per pair in keep[nPairs * TRAX_PRED_KEEP];
+// store pass (emit == true): candidates at the scanned positions candCount[].
+#define TRAX_PRED_KEEP 4
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
-                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint2* cands,
-                          uint64_t capCands, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
+                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* keep,
+                          uint2* cands, uint64_t capCands, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
                           uint32_t* launches);
 cudaError_t predict_offsets(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint32_t* nPairsDev,
                             uint64_t maxPairs, const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st,

@@ -1,0 +1,172 @@
+// trax_stages.cuh -- per-pair prediction window and per-candidate filter
+// predicate, shared by the stage-by-stage kernels and the fused batch kernel
+// so that both evaluate exactly the same float operations.
+#pragma once
+
+#include "trax_device.cuh"
+
+namespace trax {
+
+// Third-hit window of one pair (predictCount / predictStore,
+// TripletThetaPhiPredictor.h:111-185 and :286-355).  The two kernels differ
+// only in how rOrigin is rounded (Q4); both z windows are kept, the phi
+// window is common.
+struct PredWindow {
+  float zLow[2], zHigh[2];           // [0] count variant, [1] store variant
+  uint32_t zLoSec[2], zHiSec[2];
+  float phiLow, phiHigh;
+  uint32_t pL, pH, wrap;
+  bool same;                         // both variants give the same window
+};
+
+__device__ __forceinline__ void pred_z_window(const DevConfig& cfg, float p1z, float p2z, float rOrigin,
+                                              float r2t, float tip2, float minR, float maxR, float sigmaZ,
+                                              float& zLow, float& zHigh, uint32_t& lo, uint32_t& hi) {
+  const float cotTheta = div_(p2z - p1z, r2t - rOrigin);
+  float tmp = p1z + (sqrt_(maxR * maxR - tip2) - rOrigin) * cotTheta;
+  zLow = p1z + (sqrt_(minR * minR - tip2) - rOrigin) * cotTheta;
+  zHigh = (float)(tmp > zLow) * tmp + (float)(tmp < zLow) * zLow;
+  zLow = (float)(tmp > zLow) * zLow + (float)(tmp < zLow) * tmp;
+  zLow -= sigmaZ;
+  zHigh += sigmaZ;
+  lo = (uint32_t)max(f2i_sat(floor_(div_(zLow - cfg.minZ, cfg.sZ))), 0);
+  hi = min(f2u_sat(floor_(div_(zHigh - cfg.minZ, cfg.sZ))) + 1u, cfg.nZ);
+}
+
+// h1, h2: (x, y, z, phi) of the pair's hits; layer = third layer (0-based)
+__device__ __forceinline__ PredWindow pred_window(const DevConfig& cfg, uint32_t lt, uint32_t layer, float4 h1,
+                                                  float4 h2) {
+  PredWindow w;
+  const float sigmaZ = cfg.sigmaZ[lt];
+  const float sigmaPhi = cfg.sigmaPhi[lt];
+  const float minR = cfg.minR[layer];
+  const float maxR = cfg.maxR[layer];
+  const float p1x = h1.x, p1y = h1.y, p1z = h1.z;
+  const float p2x = h2.x, p2y = h2.y, p2z = h2.z;
+  float tip2 = p1y * (p2x - p1x) - p1x * (p2y - p1y);
+  tip2 *= tip2;
+  tip2 = div_(tip2, (p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
+  const float rr = p1x * p1x + p1y * p1y;
+  const float rOc = sqrt_(rr - tip2);  // :130-131
+  const float r1 = sqrt_(rr);
+  const float rOs = sqrt_(r1 * r1 - tip2);  // :305-306
+  const float r2t = sqrt_(p2x * p2x + p2y * p2y - tip2);
+  pred_z_window(cfg, p1z, p2z, rOc, r2t, tip2, minR, maxR, sigmaZ, w.zLow[0], w.zHigh[0], w.zLoSec[0], w.zHiSec[0]);
+  w.same = f2bits(rOc) == f2bits(rOs);
+  if (w.same) {
+    w.zLow[1] = w.zLow[0];
+    w.zHigh[1] = w.zHigh[0];
+    w.zLoSec[1] = w.zLoSec[0];
+    w.zHiSec[1] = w.zHiSec[0];
+  } else {
+    pred_z_window(cfg, p1z, p2z, rOs, r2t, tip2, minR, maxR, sigmaZ, w.zLow[1], w.zHigh[1], w.zLoSec[1],
+                  w.zHiSec[1]);
+  }
+  const float phi = h2.w;  // atan2(p2.y, p2.x)
+  float dPhi = phi - h1.w;
+  dPhi += (dPhi > TRAX_PI_F) ? -2 * TRAX_PI_F : (dPhi < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
+  dPhi = fabs_(dPhi);
+  const float dHits = sqrt_((p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
+  const float twoR = 2 * cfg.minRcurv;
+  const float aH = acos_(div_(dHits, twoR));
+  float tmp = fabs_(aH - cfg.acosMaxR[layer]);
+  float phiLow = fabs_(aH - cfg.acosMinR[layer]);
+  dPhi = cl_max(dPhi, cl_max(tmp, phiLow));
+  float phiHigh = phi + dPhi + sigmaPhi;
+  phiLow = phi - dPhi - sigmaPhi;
+  const bool wrapAround = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
+  phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  w.phiLow = phiLow;
+  w.phiHigh = phiHigh;
+  w.pL = f2u_sat(floor_(div_(phiLow - cfg.minPhi, cfg.sP)));
+  w.pH = min(f2u_sat(floor_(div_(phiHigh - cfg.minPhi, cfg.sP))) + 1u, cfg.nP);
+  w.wrap = wrapAround ? 1u : 0u;
+  return w;
+}
+
+// phi part of the candidate test (TripletThetaPhiPredictor.h:211-214)
+__device__ __forceinline__ bool pred_phi_ok(const PredWindow& w, float actPhi) {
+  return (!w.wrap && (w.phiLow <= actPhi && actPhi <= w.phiHigh)) ||
+         (w.wrap && ((w.phiLow <= actPhi && actPhi <= TRAX_PI_F) || (-TRAX_PI_F <= actPhi && actPhi <= w.phiHigh)));
+}
+
+__device__ __forceinline__ bool pred_valid(const PredWindow& w, int v, float4 h) {
+  const bool valid = w.zLow[v] <= h.z && h.z <= w.zHigh[v];
+  return valid && pred_phi_ok(w, h.w);
+}
+
+// Visit ranges of one z row of the third layer (the reference's j loop with
+// index = j - (j >= zEnd) * len, zEnd being the next row's start -- Q8): the
+// loop visits P1 = [J0, min(end2, zEnd)) and then P2 = [max(J0, zEnd) - len, end2 - len).
+__device__ __forceinline__ void pred_row_parts(const PredWindow& w, const uint32_t* lG, uint32_t C, uint32_t nP,
+                                               uint32_t zs, uint32_t& a1, uint32_t& b1, uint32_t& a2, uint32_t& b2) {
+  const uint32_t row = zs * (nP + 1);
+  const uint32_t zStart = cell_at(lG, row, C);
+  const uint32_t zEnd = cell_at(lG, row + nP + 1, C);
+  const uint32_t len = zEnd - zStart;
+  const uint32_t J0 = cell_at(lG, row + w.pL, C);
+  const uint32_t end2 = w.wrap * zEnd + cell_at(lG, row + w.pH, C) - w.wrap * zStart;
+  a1 = J0;
+  b1 = min(end2, zEnd);
+  if (b1 < a1) b1 = a1;
+  const uint32_t j2 = max(J0, zEnd);
+  if (j2 < end2) {
+    a2 = j2 - len;
+    b2 = end2 - len;
+  } else {
+    a2 = b2 = 0;
+  }
+}
+
+// Per-pair part of filterCount (TripletThetaPhiFilter.h:84-107): the angles
+// of the first segment and the paraboloid point of the first hit.
+struct FilterPair {
+  float theta1, phi1;
+  f3 pP1, pP2;
+  float dThetaCut, dPhiCut, tipCut;
+};
+
+__device__ __forceinline__ FilterPair filter_prep(const DevConfig& cfg, uint32_t lt, float4 A, float4 B) {
+  FilterPair f;
+  f.dThetaCut = cfg.dThetaCut[lt];
+  f.dPhiCut = cfg.dPhiCut[lt];
+  f.tipCut = cfg.tipCut[lt];
+  f.theta1 = atan2_(sqrt_((B.x - A.x) * (B.x - A.x) + (B.y - A.y) * (B.y - A.y)), (B.z - A.z));
+  f.phi1 = atan2_((B.y - A.y), (B.x - A.x));
+  f.pP1 = make_f3(A.x, A.y, A.x * A.x + A.y * A.y);
+  f.pP2 = make_f3(B.x, B.y, B.x * B.x + B.y * B.y);
+  return f;
+}
+
+// filterCount for the third hit Cc of the pair (A, B) (:84-154)
+__device__ __forceinline__ bool filter_cand(const DevConfig& cfg, const FilterPair& f, float4 B, float4 Cc) {
+  bool valid = true;
+  const float angle2 = atan2_(sqrt_((Cc.x - B.x) * (Cc.x - B.x) + (Cc.y - B.y) * (Cc.y - B.y)), (Cc.z - B.z));
+  float delta = fabs_(div_(angle2, f.theta1));
+  valid = valid && (1 - f.dThetaCut <= delta && delta <= 1 + f.dThetaCut);
+  const float phi2 = atan2_((Cc.y - B.y), (Cc.x - B.x));
+  delta = phi2 - f.phi1;
+  delta += (delta > TRAX_PI_F) ? -2 * TRAX_PI_F : (delta < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
+  valid = valid && (fabs_(delta) <= f.dPhiCut);
+  const f3 pP3 = make_f3(Cc.x, Cc.y, Cc.x * Cc.x + Cc.y * Cc.y);
+  const f3 a = sub3(f.pP2, f.pP1);
+  const f3 b = sub3(pP3, f.pP1);
+  const f3 n = normalize3(cross3(a, b));
+  const float cOx = div_(-n.x, 2 * n.z);
+  const float cOy = div_(-n.y, 2 * n.z);
+  const float cc = -(n.x * f.pP1.x + n.y * f.pP1.y + n.z * f.pP1.z);
+  const float cR = sqrt_(div_(1 - n.z * n.z - 4 * cc * n.z, 4 * n.z * n.z));
+  float vx = -cOx, vy = -cOy;
+  normalize2(vx, vy);
+  const float pCAx = cOx + cR * vx;
+  const float pCAy = cOy + cR * vy;
+  const float tip_squared = pCAx * pCAx + pCAy * pCAy;
+  valid = valid && (tip_squared <= (f.tipCut * f.tipCut));
+  valid = valid && (cR >= cfg.minRcurv);
+  return valid;
+}
+
+}  // namespace trax
