@@ -60,7 +60,9 @@ def parse():
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-parity", action="store_true")
-    p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: the workload's)")
+    p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: autotuned)")
+    p.add_argument("--no-tune", action="store_true", help="skip the autotuner (grid of the workload, default blocks)")
+    p.add_argument("--tune-cache", default=None, help="JSON cache file of the autotuner")
     return p.parse_args()
 
 
@@ -214,9 +216,15 @@ def run_ours(args, ranks):
     if args.grid:
         batch.n_z, batch.n_phi = (int(v) for v in args.grid.lower().split("x"))
     n_hits = batch.n_hits
-    cells = batch.n_events * batch.n_layers * (batch.n_z + 1) * (batch.n_phi + 1)
     ctx = capi.Context(device)
     ctx.upload(batch)
+    tune = None
+    if not args.no_tune:
+        # grid searched unless --grid fixes it; block sizes always
+        tune = ctx.autotune(cache_path=args.tune_cache, search_grid=not args.grid)
+        batch.n_z, batch.n_phi = tune["n_z"], tune["n_phi"]
+    shape = ctx.launch_config()
+    cells = batch.n_events * batch.n_layers * (batch.n_z + 1) * (batch.n_phi + 1)
     for _ in range(max(args.warmup, 3)):
         st = ctx.seed_batch(use_graph=True)
     clocks = ClockSampler(device)
@@ -263,6 +271,10 @@ def run_ours(args, ranks):
         "config": {"workload": "ttbar-like batch: 1000 events, tracks ~ Poisson(U[300,3000]), 10 layers, 6 layer "
                                "triplets, seed 2 (config 2)",
                    "events_per_gpu": batch.n_events, "hits_per_gpu": n_hits, "grid": f"{batch.n_z}x{batch.n_phi}",
+                   "block_sizes": {k: shape[k] for k in ("pair_threads", "predict_threads", "filter_threads")},
+                   "autotune": None if tune is None else {
+                       "shapes_timed": tune["shapes_timed"], "from_cache": bool(tune["from_cache"]),
+                       "best_ms": round(tune["best_ms"], 4), "default_shape_ms": round(tune["default_ms"], 4)},
                    "layer_triplets": len(batch.lts),
                    "l2": f"inputs larger than L2 ({n_hits * 28 / 1e6:.0f} MB of hit columns per step), no flush",
                    "path": "batched: one CUDA-graph replay of the whole chain per step"},

@@ -176,11 +176,46 @@ int trax_prefix_sum(trax_ctx* ctx, uint32_t* data, uint64_t n);
 int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n, void* stream, char* err_msg,
                             size_t err_len);
 
+/* Threads per block of the pair, prediction and filter kernels (multiples of
+ * 32 in [32, 256]; defaults 128, 128, 256).  No counterpart in the reference,
+ * whose work-group sizes are fixed per kernel in the run() methods (e.g.
+ * PairGeneratorBeamspot.cpp:5-183, TripletThetaPhiPredictor.cpp:10-168). */
+int trax_set_block_sizes(trax_ctx* ctx, uint32_t pair_threads, uint32_t predict_threads, uint32_t filter_threads);
+/* out5 = n_z, n_phi, pair threads, prediction threads, filter threads. */
+int trax_get_launch_config(trax_ctx* ctx, uint32_t* out5);
+
 /* ------------------------------------------------------------- batched
  * The whole chain (buildTriplets, TripletBuilder.cpp:312-467) for all
  * uploaded events in one pass of batched launches, optionally replayed from a
  * CUDA graph. */
 int trax_seed_batch(trax_ctx* ctx, const trax_batch_opts* opts, trax_batch_stats* stats);
+
+/* Autotuner of the batched chain's launch shape.  No counterpart in the
+ * reference, where the grid size is a command-line parameter
+ * (grid.nSectorsZ / grid.nSectorsPhi, TripletBuilder.cpp:631-634) and work-group sizes
+ * are fixed.  It times CUDA-graph replays of trax_seed_batch on the uploaded
+ * hits for grid sizes n_z x n_phi (cells per layer within the shared-memory
+ * grid build) and then for the three kernels' block sizes, one coordinate at
+ * a time, and leaves the fastest shape set on the context.  The result is
+ * cached in the JSON file `cache_path` (may be NULL: no cache), keyed by a
+ * hash of the workload (batch shape, layer triplets, geometry, minimum pT,
+ * whether linking runs) and the GPU's SM count; a cached shape is applied
+ * without timing.  The chosen grid changes the grid-ordered hit indices of
+ * the results, not the triplets in input-hit terms. */
+typedef struct trax_tune_opts {
+  int search_grid; /* 1: search n_z x n_phi; 0: keep the context's grid */
+  int run_linking; /* time the chain with linking (1) or up to the filter (0) */
+  int replays;     /* timed graph replays per shape (best one counts); 0 -> 3 */
+} trax_tune_opts;
+typedef struct trax_tune_result {
+  uint32_t n_z, n_phi;
+  uint32_t pair_threads, predict_threads, filter_threads;
+  uint32_t from_cache;       /* 1: taken from the cache file */
+  uint32_t shapes_timed;     /* shapes timed by this call */
+  double best_ms;            /* device time of one chain replay at the chosen shape */
+  double default_ms;         /* the same for the shape the context had before */
+} trax_tune_result;
+int trax_autotune(trax_ctx* ctx, const char* cache_path, const trax_tune_opts* opts, trax_tune_result* result);
 
 /* Device time of the last run, from CUDA events on the context's stream
  * (RuntimeRecord's per-stage count/scan/store classes, RuntimeRecord.cpp:123-192):

@@ -1,0 +1,90 @@
+"""Launch shapes: block sizes, grid sizes around the shared-memory grid-build
+limit, and the autotuner (trax_autotune) with its JSON cache.  Whatever shape
+runs, the results must equal the oracle's at the same grid."""
+import json
+
+import numpy as np
+import pytest
+
+from trax_gb300 import events
+
+from .test_gpu_parity import compare
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx(trax_lib):
+    c = trax_lib.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("blocks", [(64, 64, 128), (256, 256, 64), (96, 160, 224)])
+def test_block_sizes_keep_results(ctx, oracle_lib, blocks):
+    batch = events.generate(2, n_events=3)
+    ref = oracle_lib.run(batch)[0]
+    ctx.upload(batch)
+    ctx.set_block_sizes(*blocks)
+    try:
+        ctx.seed_batch(use_graph=True)
+        compare(ctx.results(), ref)
+    finally:
+        ctx.set_block_sizes(128, 128, 256)
+
+
+@pytest.mark.parametrize("grid", [(190, 128), (400, 128), (200, 256), (500, 128)])
+def test_grid_sizes_around_shared_memory_limit(ctx, oracle_lib, grid):
+    # (400, 128) and (200, 256) fill most of the shared-memory counters,
+    # (500, 128) has more cells than fit and counts in global memory
+    batch = events.generate(2, n_events=3)
+    batch.n_z, batch.n_phi = grid
+    ref = oracle_lib.run(batch)[0]
+    ctx.upload(batch)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
+def test_invalid_block_sizes_rejected(ctx, trax_lib):
+    for bad in [(0, 128, 128), (33, 128, 128), (128, 512, 128), (128, 128, 16)]:
+        with pytest.raises(trax_lib.TraxError) as e:
+            ctx.set_block_sizes(*bad)
+        assert e.value.code == 2
+
+
+def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
+    batch = events.generate(1, n_events=20)
+    cache = tmp_path / "tune.json"
+    c = trax_lib.Context(0)
+    try:
+        c.upload(batch)
+        res = c.autotune(cache_path=str(cache), search_grid=True, replays=1)
+        assert res["from_cache"] == 0 and res["shapes_timed"] > 1
+        assert 0 < res["best_ms"] <= res["default_ms"]
+        shape = c.launch_config()
+        assert (shape["n_z"], shape["n_phi"]) == (res["n_z"], res["n_phi"])
+        assert (shape["n_z"] + 1) * (shape["n_phi"] + 1) <= 53248
+        # results at the tuned shape equal the oracle's at the tuned grid
+        batch.n_z, batch.n_phi = res["n_z"], res["n_phi"]
+        ref = oracle_lib.run(batch)[0]
+        c.seed_batch(use_graph=True)
+        compare(c.results(), ref)
+        entries = json.loads(cache.read_text())["entries"]
+        assert len(entries) == 1 and entries[0]["n_z"] == res["n_z"] and entries[0]["sm_count"] > 0
+    finally:
+        c.close()
+    # a new context with the same workload takes the cached shape without timing
+    c = trax_lib.Context(0)
+    try:
+        c.upload(events.generate(1, n_events=20))
+        res2 = c.autotune(cache_path=str(cache), search_grid=True, replays=1)
+        assert res2["from_cache"] == 1 and res2["shapes_timed"] == 0
+        assert [res2[k] for k in ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads")] == \
+               [res[k] for k in ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads")]
+        # a different workload gets its own entry
+        c.upload(events.generate(1, n_events=21))
+        res3 = c.autotune(cache_path=str(cache), search_grid=False, replays=1)
+        assert res3["from_cache"] == 0
+        assert len(json.loads(cache.read_text())["entries"]) == 2
+    finally:
+        c.close()

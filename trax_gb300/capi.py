@@ -28,7 +28,8 @@ EXPORTED = [
     "trax_triplet_predict", "trax_triplet_filter", "trax_connectivity", "trax_circle_fit",
     "trax_cellular_automaton", "trax_prefix_sum", "trax_seed_batch", "trax_get_stats", "trax_get_pairs",
     "trax_get_timings", "trax_get_candidates", "trax_get_triplets", "trax_get_triplet_eta_pt", "trax_get_links",
-    "trax_get_tracks", "trax_get_grid", "trax_get_hit_perm",
+    "trax_get_tracks", "trax_get_grid", "trax_get_hit_perm", "trax_set_block_sizes", "trax_get_launch_config",
+    "trax_autotune",
 ]
 
 
@@ -61,6 +62,16 @@ class BatchStatsC(ctypes.Structure):
         "n_hits", "n_pairs", "n_candidates", "n_triplets", "n_links", "n_connectable", "n_non_connectable",
         "n_track_entries", "n_pair_sentinels", "n_candidate_sentinels", "kernel_launches")] + [
         ("device_ms", ctypes.c_double)]
+
+
+class TuneOptsC(ctypes.Structure):
+    _fields_ = [("search_grid", ctypes.c_int), ("run_linking", ctypes.c_int), ("replays", ctypes.c_int)]
+
+
+class TuneResultC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint32) for n in (
+        "n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "from_cache", "shapes_timed")] + [
+        ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
 
 
 _lock = threading.Lock()
@@ -112,6 +123,9 @@ def load() -> ctypes.CDLL:
             "trax_get_tracks": ([vp, vp, vp, vp], i32),
             "trax_get_grid": ([vp, vp, pu64], i32),
             "trax_get_hit_perm": ([vp, vp], i32),
+            "trax_set_block_sizes": ([vp, u32, u32, u32], i32),
+            "trax_get_launch_config": ([vp, vp], i32),
+            "trax_autotune": ([vp, ctypes.c_char_p, vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -255,6 +269,26 @@ class Context:
         st = BatchStatsC()
         self._check(self._L.trax_seed_batch(self._h, ctypes.byref(opts), ctypes.byref(st)))
         return BatchStats(*[getattr(st, f[0]) for f in BatchStatsC._fields_])
+
+    def set_block_sizes(self, pair_threads: int, predict_threads: int, filter_threads: int):
+        self._check(self._L.trax_set_block_sizes(self._h, pair_threads, predict_threads, filter_threads))
+
+    def launch_config(self) -> Dict[str, int]:
+        """Current grid and block sizes: n_z, n_phi, pair/predict/filter threads."""
+        a = np.zeros(5, dtype=np.uint32)
+        self._check(self._L.trax_get_launch_config(self._h, _p(a)))
+        return dict(zip(("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads"), a.tolist()))
+
+    def autotune(self, cache_path: Optional[str] = None, search_grid: bool = True, run_linking: bool = True,
+                 replays: int = 3) -> Dict[str, float]:
+        """trax_autotune: time graph replays over grid and block sizes, keep the fastest."""
+        opts = TuneOptsC(int(search_grid), int(run_linking), int(replays))
+        res = TuneResultC()
+        path = None if cache_path is None else os.fsencode(cache_path)
+        self._check(self._L.trax_autotune(self._h, path, ctypes.byref(opts), ctypes.byref(res)))
+        out = {f[0]: getattr(res, f[0]) for f in TuneResultC._fields_}
+        self.n_z, self.n_phi = out["n_z"], out["n_phi"]
+        return out
 
     def stats(self) -> BatchStats:
         st = BatchStatsC()

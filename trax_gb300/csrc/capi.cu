@@ -99,6 +99,7 @@ struct trax_ctx {
   float minPt = 0.0f;
   std::vector<float> minR, maxR;
   uint32_t nZ = 0, nP = 0;
+  uint32_t pairThreads = 128, predThreads = 128, filterThreads = 256;  // launch shape
   bool haveLT = false, haveGeom = false, haveGrid = false, haveHits = false;
   // batch shape
   uint32_t E = 0, L = 0, nHits = 0;
@@ -259,6 +260,9 @@ int build_config(trax_ctx* c) {
   g.sP = (MAX_PHI - MIN_PHI) / (float)c->nP;
   g.minRcurv = min_radius_curvature(c->minPt);
   g.dEtaCut = c->dEtaCut;
+  g.pairThreads = c->pairThreads;
+  g.predThreads = c->predThreads;
+  g.filterThreads = c->filterThreads;
   for (uint32_t p = 0; p < g.nLT; ++p) {
     const trax_layer_triplet& t = c->lts[p];
     if (t.layer1 < 1 || t.layer2 < 1 || t.layer3 < 1 || t.layer1 > c->L || t.layer2 > c->L || t.layer3 > c->L)
@@ -345,7 +349,7 @@ int stage_grid(trax_ctx* c, Mode mode) {
   ENSURE(player, n, 4); ENSURE(pdet, n, 4); ENSURE(phid, n, 4); ENSURE(pevt, n, 4); ENSURE(porig, n, 4);
   ENSURE(pxyzp, n, 16);
   ENSURE(sc_cell, n, 4); ENSURE(sc_phi, n, 4); ENSURE(sc_perm, n, 4);
-  if (c->cfg.C > 24576) ENSURE(sc_counts, cells, 4);
+  if (c->cfg.C > TRAX_GRID_SMEM_CELLS) ENSURE(sc_counts, cells, 4);
   GridInput in;
   in.x = ptr<float>(c->in_x);
   in.y = ptr<float>(c->in_y);
@@ -699,6 +703,41 @@ uint64_t shape_key(trax_ctx* c, bool linking) {
   return k;
 }
 
+}  // namespace
+
+namespace trax {
+
+// Hash of what determines the best launch shape: batch shape, layer
+// triplets, geometry and minimum pT (not the grid or block sizes).
+uint64_t workload_hash(const trax_ctx* c) {
+  uint64_t k = 1469598103934665603ull;
+  auto mix = [&k](const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) {
+      k ^= b[i];
+      k *= 1099511628211ull;
+    }
+  };
+  mix(&c->E, sizeof(c->E));
+  mix(&c->L, sizeof(c->L));
+  mix(&c->nHits, sizeof(c->nHits));
+  mix(&c->minPt, sizeof(c->minPt));
+  if (!c->lts.empty()) mix(c->lts.data(), c->lts.size() * sizeof(trax_layer_triplet));
+  if (!c->minR.empty()) mix(c->minR.data(), c->minR.size() * sizeof(float));
+  if (!c->maxR.empty()) mix(c->maxR.data(), c->maxR.size() * sizeof(float));
+  return k;
+}
+
+int ctx_device(const trax_ctx* c) { return c->device; }
+
+bool ctx_ready(const trax_ctx* c) { return c->haveLT && c->haveGeom && c->haveGrid && c->haveHits; }
+
+void ctx_set_error(trax_ctx* c, const char* msg) { c->err = msg; }
+
+}  // namespace trax
+
+namespace {
+
 int run_synced_chain(trax_ctx* c, bool linking) {
   for (int s = 1; s <= (linking ? 7 : 4); ++s) RC(run_stage(c, s));
   return TRAX_OK;
@@ -818,6 +857,27 @@ int trax_set_grid(trax_ctx* c, uint32_t n_z, uint32_t n_phi) {
   c->nP = n_phi;
   c->haveGrid = true;
   c->stage = 0;
+  return TRAX_OK;
+}
+
+int trax_set_block_sizes(trax_ctx* c, uint32_t pair_threads, uint32_t predict_threads, uint32_t filter_threads) {
+  if (!c) return TRAX_ERR_ARG;
+  for (uint32_t t : {pair_threads, predict_threads, filter_threads})
+    if (t < 32 || t > TRAX_MAX_TUNED_THREADS || t % 32)
+      return fail(c, TRAX_ERR_ARG, "block sizes must be multiples of 32 in [32, 256]");
+  c->pairThreads = pair_threads;
+  c->predThreads = predict_threads;
+  c->filterThreads = filter_threads;
+  return TRAX_OK;
+}
+
+int trax_get_launch_config(trax_ctx* c, uint32_t* out5) {
+  if (!c || !out5) return TRAX_ERR_ARG;
+  out5[0] = c->nZ;
+  out5[1] = c->nP;
+  out5[2] = c->pairThreads;
+  out5[3] = c->predThreads;
+  out5[4] = c->filterThreads;
   return TRAX_OK;
 }
 

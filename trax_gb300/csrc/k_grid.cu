@@ -18,8 +18,9 @@ namespace {
 
 constexpr int GRID_THREADS = 256;
 constexpr int GRID_WARPS = GRID_THREADS / 32;
-// cell counters live in shared memory up to this many cells
-constexpr uint32_t GRID_SMEM_CELLS = 24576;  // 96 KB
+// cell counters live in shared memory up to TRAX_GRID_SMEM_CELLS cells (208 KB,
+// one CTA per SM at the largest grids); larger grids count in global memory
+constexpr uint32_t GRID_SMEM_CELLS = TRAX_GRID_SMEM_CELLS;
 
 __global__ void __launch_bounds__(GRID_THREADS)
     grid_kernel(DevConfig cfg, GridInput in, uint32_t* __restrict__ grid, DevHits out, GridScratch sc,

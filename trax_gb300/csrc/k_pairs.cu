@@ -24,7 +24,6 @@ namespace trax {
 
 namespace {
 
-constexpr int PAIR_THREADS = 128;
 
 struct PairWindow {
   float zLow, zHigh, phiLow, phiHigh;
@@ -140,7 +139,7 @@ __global__ void segments_kernel(DevConfig cfg, const uint32_t* __restrict__ grid
 }
 
 template <bool EMIT>
-__global__ void __launch_bounds__(PAIR_THREADS)
+__global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     pair_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                 const uint32_t* __restrict__ segOuter, const uint32_t* __restrict__ taskBase,
                 const uint32_t* __restrict__ nTasksDev, uint32_t* taskCount, uint2* pairs, uint32_t capPairs,
@@ -247,7 +246,7 @@ __global__ void pair_offsets_kernel(DevConfig cfg, const uint32_t* taskBase, con
 
 int grid_for(uint64_t items, int threads) {
   uint64_t blocks = (items + threads - 1) / threads;
-  uint64_t cap = (uint64_t)sm_count() * 16;
+  uint64_t cap = (uint64_t)sm_count() * (4096 / threads);  // two waves at full occupancy
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   return (int)blocks;
@@ -269,12 +268,13 @@ cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, De
                        uint32_t* launches) {
   const uint32_t cap = capPairs > 0xffffffffull ? 0xffffffffu : (uint32_t)capPairs;
   if (emit && maxTasks == 0) return cudaSuccess;
-  const int blocks = grid_for(maxTasks + 1, PAIR_THREADS);
+  const int threads = (int)cfg.pairThreads;
+  const int blocks = grid_for(maxTasks + 1, threads);
   if (emit)
-    pair_kernel<true><<<blocks, PAIR_THREADS, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
+    pair_kernel<true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
                                                        taskCount, pairs, cap, sentinels, err);
   else
-    pair_kernel<false><<<blocks, PAIR_THREADS, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
+    pair_kernel<false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
                                                         taskCount, pairs, cap, sentinels, err);
   if (launches) *launches += 1;
   return cudaGetLastError();

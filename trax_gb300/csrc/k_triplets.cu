@@ -19,11 +19,10 @@ namespace trax {
 
 namespace {
 
-constexpr int PRED_THREADS = 128;
 
 int grid_for(uint64_t items, int threads) {
   uint64_t blocks = (items + threads - 1) / threads;
-  uint64_t cap = (uint64_t)sm_count() * 16;
+  uint64_t cap = (uint64_t)sm_count() * (4096 / threads);  // two waves at full occupancy
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
   return (int)blocks;
@@ -33,7 +32,7 @@ int grid_for(uint64_t items, int threads) {
 // min(count, TRAX_PRED_KEEP) candidates the store pass would write (the store
 // variant's valid hits, capped at the count; slots it would leave unwritten
 // get the sentinel), so that the store pass is a copy for most pairs.
-__global__ void __launch_bounds__(PRED_THREADS)
+__global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     predict_count_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
                          const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev, uint32_t* candCount,
@@ -86,7 +85,7 @@ __global__ void __launch_bounds__(PRED_THREADS)
 // Store pass (predictStore, :358-402): candidates (pair, hit3) at the
 // scanned position; copied from the captured slots, re-walked only when a
 // pair has more candidates than slots.
-__global__ void __launch_bounds__(PRED_THREADS)
+__global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     predict_store_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
                          const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev,
@@ -218,13 +217,14 @@ cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid,
                           uint32_t* launches) {
   (void)err;
   const uint32_t cap = capCands > 0xffffffffull ? 0xffffffffu : (uint32_t)capCands;
-  const int blocks = grid_for(maxPairs + 1, PRED_THREADS);
+  const int threads = (int)cfg.predThreads;
+  const int blocks = grid_for(maxPairs + 1, threads);
   if (emit) {
     if (maxPairs == 0) return cudaSuccess;
-    predict_store_kernel<<<blocks, PRED_THREADS, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+    predict_store_kernel<<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
                                                           nPairsDev, candCount, keep, cands, cap, sentinels);
   } else {
-    predict_count_kernel<<<blocks, PRED_THREADS, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+    predict_count_kernel<<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
                                                           nPairsDev, candCount, keep);
   }
   if (launches) *launches += 1;
@@ -250,7 +250,7 @@ cudaError_t predict_offsets(const DevConfig& cfg, DevHits hits, const uint2* pai
 cudaError_t filter_candidates(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint2* cands,
                               const uint32_t* nCandsDev, uint64_t maxCands, uint32_t* flags, cudaStream_t st,
                               uint32_t* launches) {
-  filter_kernel<<<grid_for(maxCands + 1, 256), 256, 0, st>>>(cfg, hits.xyzp, hits.layer, pairs, cands, nCandsDev,
+  filter_kernel<<<grid_for(maxCands + 1, (int)cfg.filterThreads), (int)cfg.filterThreads, 0, st>>>(cfg, hits.xyzp, hits.layer, pairs, cands, nCandsDev,
                                                               flags);
   if (launches) *launches += 1;
   return cudaGetLastError();

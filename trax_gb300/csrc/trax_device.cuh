@@ -32,7 +32,12 @@ struct DevConfig {
   // acos(r / (2 minRadiusCurvature)) of each layer's min/max radius, computed on
   // the host with the same trax_math.h code as the kernels would
   float acosMinR[TRAX_MAX_LAYERS], acosMaxR[TRAX_MAX_LAYERS];
+  // launch shape chosen by the autotuner (threads per block of the pair,
+  // prediction and filter kernels; at most TRAX_MAX_TUNED_THREADS)
+  uint32_t pairThreads, predThreads, filterThreads;
 };
+
+#define TRAX_MAX_TUNED_THREADS 256
 
 // Grid-ordered hit collection (the reference's HitCollection after GridBuilder).
 struct DevHits {

@@ -9,6 +9,8 @@
 
 #include "trax_device.cuh"
 
+struct trax_ctx;
+
 namespace trax {
 
 // ---------------------------------------------------------------- scans
@@ -65,6 +67,10 @@ cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const u
 // TRAX_PRED_KEEP captured candidates per pair in keep[nPairs * TRAX_PRED_KEEP];
 // store pass (emit == true): candidates at the scanned positions candCount[].
 #define TRAX_PRED_KEEP 4
+
+// grids of up to this many cells per layer are built with shared-memory
+// counters (4 bytes per cell)
+#define TRAX_GRID_SMEM_CELLS 53248u
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
                           const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* keep,
                           uint2* cands, uint64_t capCands, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
@@ -139,5 +145,11 @@ cudaError_t ca_tracks(CABuffers b, const uint32_t* nTDev, uint64_t maxT, uint32_
 
 // number of SMs of the current device (cached)
 int sm_count();
+
+// context hooks for the autotuner (capi.cu)
+uint64_t workload_hash(const trax_ctx* c);
+int ctx_device(const trax_ctx* c);
+bool ctx_ready(const trax_ctx* c);
+void ctx_set_error(trax_ctx* c, const char* msg);
 
 }  // namespace trax

@@ -1,0 +1,242 @@
+// tune.cu -- launch-shape autotuner of the batched chain (trax_autotune).
+//
+// The tuner is a client of the C ABI: it sets a shape (trax_set_grid,
+// trax_set_block_sizes), runs trax_seed_batch with a CUDA graph (the first
+// call of a shape calibrates and captures, the replays are timed with CUDA
+// events on the context's stream) and keeps the fastest.  The grid is
+// searched first with the current block sizes, then each kernel's block size
+// in turn.  Results go to a small JSON cache keyed by the workload hash and
+// the SM count.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "trax/trax.h"
+#include "trax_kernels.h"
+
+namespace {
+
+struct Shape {
+  uint32_t nZ, nP, pairT, predT, filtT;
+};
+
+// Device milliseconds of one replay at `s` (best of `replays`), or a negative
+// value when the shape cannot run (its status is returned in *rc).
+double time_shape(trax_ctx* c, const Shape& s, bool linking, int replays, int* rc) {
+  *rc = trax_set_grid(c, s.nZ, s.nP);
+  if (*rc == TRAX_OK) *rc = trax_set_block_sizes(c, s.pairT, s.predT, s.filtT);
+  if (*rc != TRAX_OK) return -1.0;
+  trax_batch_opts o;
+  o.use_graph = 1;
+  o.run_linking = linking ? 1 : 0;
+  o.d_eta_cut = 0.0f;  // keep the context's cut
+  trax_batch_stats st;
+  *rc = trax_seed_batch(c, &o, &st);  // calibration + capture + first replay
+  if (*rc != TRAX_OK) return -1.0;
+  double best = st.device_ms;
+  for (int r = 0; r < replays; ++r) {
+    *rc = trax_seed_batch(c, &o, &st);
+    if (*rc != TRAX_OK) return -1.0;
+    best = std::min(best, st.device_ms);
+  }
+  return best;
+}
+
+std::string hex64(uint64_t v) {
+  char b[24];
+  snprintf(b, sizeof(b), "%016llx", (unsigned long long)v);
+  return b;
+}
+
+// ------------------------------------------------------------ JSON cache
+// {"trax_autotune": 1, "entries": [ {"key": "...", "sm_count": N, "n_z": ...}, ... ]}
+// Entries are flat objects of numbers plus the key string.
+
+std::vector<std::string> read_entries(const char* path) {
+  std::vector<std::string> out;
+  std::ifstream f(path);
+  if (!f) return out;
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string s = ss.str();
+  size_t at = s.find("\"entries\"");
+  if (at == std::string::npos) return out;
+  at = s.find('[', at);
+  while (at != std::string::npos) {
+    const size_t a = s.find('{', at);
+    if (a == std::string::npos) break;
+    const size_t b = s.find('}', a);
+    if (b == std::string::npos) break;
+    out.push_back(s.substr(a, b - a + 1));
+    at = b + 1;
+  }
+  return out;
+}
+
+bool field_u64(const std::string& obj, const char* name, unsigned long long* v) {
+  const std::string k = std::string("\"") + name + "\"";
+  size_t p = obj.find(k);
+  if (p == std::string::npos) return false;
+  p = obj.find(':', p);
+  if (p == std::string::npos) return false;
+  return sscanf(obj.c_str() + p + 1, " %llu", v) == 1;
+}
+
+bool field_f64(const std::string& obj, const char* name, double* v) {
+  const std::string k = std::string("\"") + name + "\"";
+  size_t p = obj.find(k);
+  if (p == std::string::npos) return false;
+  p = obj.find(':', p);
+  if (p == std::string::npos) return false;
+  return sscanf(obj.c_str() + p + 1, " %lf", v) == 1;
+}
+
+bool entry_key(const std::string& obj, std::string* key) {
+  size_t p = obj.find("\"key\"");
+  if (p == std::string::npos) return false;
+  p = obj.find('"', obj.find(':', p));
+  if (p == std::string::npos) return false;
+  const size_t q = obj.find('"', p + 1);
+  if (q == std::string::npos) return false;
+  *key = obj.substr(p + 1, q - p - 1);
+  return true;
+}
+
+bool cache_lookup(const char* path, const std::string& key, Shape* s, double* ms) {
+  for (const std::string& e : read_entries(path)) {
+    std::string k;
+    if (!entry_key(e, &k) || k != key) continue;
+    unsigned long long v[5];
+    if (!field_u64(e, "n_z", &v[0]) || !field_u64(e, "n_phi", &v[1]) || !field_u64(e, "pair_threads", &v[2]) ||
+        !field_u64(e, "predict_threads", &v[3]) || !field_u64(e, "filter_threads", &v[4]))
+      continue;
+    *s = Shape{(uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3], (uint32_t)v[4]};
+    if (!field_f64(e, "ms", ms)) *ms = 0.0;
+    return true;
+  }
+  return false;
+}
+
+bool cache_store(const char* path, const std::string& key, int sms, const Shape& s, double ms) {
+  std::vector<std::string> keep;
+  for (const std::string& e : read_entries(path)) {
+    std::string k;
+    if (entry_key(e, &k) && k != key) keep.push_back(e);
+  }
+  char b[512];
+  snprintf(b, sizeof(b),
+           "{\"key\": \"%s\", \"sm_count\": %d, \"n_z\": %u, \"n_phi\": %u, \"pair_threads\": %u, "
+           "\"predict_threads\": %u, \"filter_threads\": %u, \"ms\": %.6f}",
+           key.c_str(), sms, s.nZ, s.nP, s.pairT, s.predT, s.filtT, ms);
+  keep.push_back(b);
+  const std::string tmp = std::string(path) + ".tmp";
+  {
+    std::ofstream f(tmp, std::ios::trunc);
+    if (!f) return false;
+    f << "{\"trax_autotune\": 1, \"entries\": [\n";
+    for (size_t i = 0; i < keep.size(); ++i) f << "  " << keep[i] << (i + 1 < keep.size() ? ",\n" : "\n");
+    f << "]}\n";
+    if (!f) return false;
+  }
+  return std::rename(tmp.c_str(), path) == 0;
+}
+
+}  // namespace
+
+extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tune_opts* opts,
+                             trax_tune_result* result) {
+  if (!c) return TRAX_ERR_ARG;
+  if (!trax::ctx_ready(c)) {
+    trax::ctx_set_error(c, "layer triplets, geometry, grid and hits must be set before tuning");
+    return TRAX_ERR_STATE;
+  }
+  const bool searchGrid = opts ? opts->search_grid != 0 : true;
+  const bool linking = opts ? opts->run_linking != 0 : true;
+  const int replays = (opts && opts->replays > 0) ? opts->replays : 3;
+  if (cudaSetDevice(trax::ctx_device(c)) != cudaSuccess) {
+    trax::ctx_set_error(c, "cudaSetDevice failed");
+    return TRAX_ERR_CUDA;
+  }
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, trax::ctx_device(c));
+
+  uint32_t cur[5];
+  int rc = trax_get_launch_config(c, cur);
+  if (rc != TRAX_OK) return rc;
+  const Shape start{cur[0], cur[1], cur[2], cur[3], cur[4]};
+
+  uint64_t h = trax::workload_hash(c);
+  h ^= (uint64_t)sms * 0x9e3779b97f4a7c15ull;
+  h ^= linking ? 0x5bd1e995ull : 0ull;
+  h ^= searchGrid ? 0 : ((uint64_t)start.nZ << 40) ^ ((uint64_t)start.nP << 20);
+  const std::string key = hex64(h);
+
+  trax_tune_result res;
+  memset(&res, 0, sizeof(res));
+  Shape best = start;
+  double bestMs = -1.0;
+  if (cache_path && cache_lookup(cache_path, key, &best, &bestMs)) {
+    rc = trax_set_grid(c, best.nZ, best.nP);
+    if (rc == TRAX_OK) rc = trax_set_block_sizes(c, best.pairT, best.predT, best.filtT);
+    if (rc != TRAX_OK) return rc;
+    res.from_cache = 1;
+    res.best_ms = bestMs;
+    res.default_ms = -1.0;
+  } else {
+    int shapeRc = TRAX_OK;
+    const double startMs = time_shape(c, start, linking, replays, &shapeRc);
+    if (startMs < 0) return shapeRc;  // the context's own shape must run
+    res.shapes_timed = 1;
+    res.default_ms = startMs;
+    best = start;
+    bestMs = startMs;
+    auto consider = [&](const Shape& s) {
+      const double ms = time_shape(c, s, linking, replays, &shapeRc);
+      ++res.shapes_timed;
+      if (ms >= 0 && ms < bestMs) {
+        bestMs = ms;
+        best = s;
+      }
+    };
+    if (searchGrid) {
+      static const uint32_t zs[] = {50, 100, 150, 200, 300, 400};
+      static const uint32_t ps[] = {64, 128, 256};
+      for (uint32_t z : zs)
+        for (uint32_t p : ps) {
+          if ((z + 1) * (p + 1) > TRAX_GRID_SMEM_CELLS) continue;
+          if (z == start.nZ && p == start.nP) continue;
+          consider(Shape{z, p, best.pairT, best.predT, best.filtT});
+        }
+    }
+    static const uint32_t ts[] = {64, 128, 256};
+    for (int k = 0; k < 3; ++k)
+      for (uint32_t t : ts) {
+        Shape s = best;
+        uint32_t* f = k == 0 ? &s.pairT : k == 1 ? &s.predT : &s.filtT;
+        if (*f == t) continue;
+        *f = t;
+        consider(s);
+      }
+    rc = trax_set_grid(c, best.nZ, best.nP);
+    if (rc == TRAX_OK) rc = trax_set_block_sizes(c, best.pairT, best.predT, best.filtT);
+    if (rc != TRAX_OK) return rc;
+    res.best_ms = bestMs;
+    if (cache_path && !cache_store(cache_path, key, sms, best, bestMs)) {
+      trax::ctx_set_error(c, "could not write the autotune cache file");
+      return TRAX_ERR_ARG;
+    }
+  }
+  res.n_z = best.nZ;
+  res.n_phi = best.nP;
+  res.pair_threads = best.pairT;
+  res.predict_threads = best.predT;
+  res.filter_threads = best.filtT;
+  if (result) *result = res;
+  return TRAX_OK;
+}
