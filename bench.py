@@ -148,17 +148,18 @@ def peaks():
 
 
 # Algorithmic bytes of the timed kernels: compulsory streams only (each input
-# array read once, each output written once), from the sizes of the run.
+# array read once, each output written once), from the sizes of the run.  The
+# packed (x, y, z, phi) hit array is 16 B per hit, the grid 4 B per cell.
 def kernel_bytes(name, st, n_tasks, n_hits, cells):
     P, Cc, T = st.n_pairs, st.n_candidates, st.n_triplets
     return {
         "grid_build": 56 * n_hits + 4 * cells,
-        "pair_count": 16 * n_tasks + 4 * n_tasks,
-        "pair_store": 16 * n_tasks + 8 * n_tasks + 8 * P,
-        "predict_count": 8 * P + 4 * P,
-        "predict_store": 8 * P + 8 * P + 8 * Cc,
-        "filter": 8 * Cc + 4 * Cc,
-        "filter_store": 8 * Cc + 8 * Cc + 12 * T,
+        "pair_count": 16 * n_hits + 4 * cells + 4 * n_tasks,
+        "pair_store": 16 * n_hits + 4 * cells + 4 * n_tasks + 8 * P,
+        "predict_count": 16 * n_hits + 4 * cells + 8 * P + 4 * P,
+        "predict_store": 8 * P + 4 * P + 8 * Cc,
+        "filter": 16 * n_hits + 8 * P + 8 * Cc + 4 * Cc,
+        "filter_store": 8 * P + 8 * Cc + 4 * Cc + 12 * T,
         "connectivity_count": 12 * T + 4 * T + 4 * T,
         "connectivity_store": 12 * T + 8 * st.n_links,
     }.get(name, 0)

@@ -298,17 +298,24 @@ int read_slots(trax_ctx* c) {
   return TRAX_OK;
 }
 
+int error_from_bits(trax_ctx* c, uint32_t bits);
+
+// a stage total read by the host in SYNCED mode; the error word comes along so
+// that an overflowed or timed-out scan stops the chain before its total is used
 int read_slot(trax_ctx* c, int k, uint64_t* out) {
   CK(cudaMemcpyAsync(c->hSlots + k, slot(c, k), sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(c->hSlots + S_ERR, slot(c, S_ERR), sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   *out = c->hSlots[k];
-  return TRAX_OK;
+  return error_from_bits(c, c->hSlots[S_ERR] & (TRAX_EBIT_OVERFLOW | TRAX_EBIT_TIMEOUT));
 }
 
 int error_from_bits(trax_ctx* c, uint32_t bits) {
   if (bits & TRAX_EBIT_TIMEOUT) return fail(c, TRAX_ERR_TIMEOUT, "a bounded device wait ran out");
   if (bits & TRAX_EBIT_CAPACITY) return fail(c, TRAX_ERR_CAPACITY, "a stage produced more items than its capacity");
   if (bits & TRAX_EBIT_BOUNDS) return fail(c, TRAX_ERR_DEVICE_ASSERT, "a device-side bounds check fired");
+  if (bits & TRAX_EBIT_OVERFLOW)
+    return fail(c, TRAX_ERR_CAPACITY, "a stage's item count does not fit the 32-bit index space");
   return TRAX_OK;
 }
 
@@ -335,7 +342,8 @@ int scan_publish(trax_ctx* c, Mode mode, uint32_t* data, uint64_t nHost, const u
   if (mode == SYNCED) CK(ensure(c, c->scanScratch, scan_scratch_bytes(maxN)));
   else if (scan_scratch_bytes(maxN) > c->scanScratch.cap)
     return fail(c, TRAX_ERR_STATE, "device-mode scan scratch too small");
-  CK(scan_exclusive(data, data, nHost + 1, nDev, 1, maxN, c->scanScratch.p, dev_err(c), c->st, &c->launches));
+  CK(scan_exclusive(data, data, nHost + 1, nDev, 1, maxN, c->scanScratch.p, dev_err(c), c->st, &c->launches,
+                    true));
   CK(publish_total(data, nDev, nHost, cap, slot(c, dst), dev_err(c), c->st, &c->launches));
   return TRAX_OK;
 }
@@ -435,8 +443,8 @@ int stage_predict(trax_ctx* c, Mode mode) {
                    candCount, ptr<uint32_t>(c->predKeep), ptr<uint2>(c->cands), maxCands, slot(c, S_CAND_SENT),
                    dev_err(c), c->st, &c->launches));
   KEND(TK_PRED_EMIT);
-  CK(predict_offsets(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs, candCount,
-                     ptr<uint32_t>(c->candOffsets), c->st, &c->launches));
+  CK(predict_offsets(c->cfg, ptr<uint32_t>(c->pairOffsets), nPairsDev, candCount, ptr<uint32_t>(c->candOffsets), c->st,
+                     &c->launches));
   return TRAX_OK;
 }
 
@@ -583,7 +591,7 @@ int stage_ca(trax_ctx* c, Mode mode) {
   // in-degree prefix (its total is the number of links; not published)
   if (mode == SYNCED) CK(ensure(c, c->scanScratch, scan_scratch_bytes(maxT + 1)));
   CK(scan_exclusive(b.inStart, b.inStart, c->nT + 1, mode == DEVICE ? nTDev : nullptr, 1, maxT + 1,
-                    c->scanScratch.p, dev_err(c), c->st, &c->launches));
+                    c->scanScratch.p, dev_err(c), c->st, &c->launches, true));
   CK(ca_fill(ptr<uint32_t>(c->follower), nLinksDev, maxLinks, b, nTDev, maxT, c->st, &c->launches));
   CK(ca_forward(c->cfg, ptr<uint32_t>(c->basis), b, nTDev, maxT, c->st, &c->launches));
   CK(ca_backward(ptr<uint32_t>(c->basis), ptr<float>(c->pt), b, nTDev, maxT, nLinksDev, c->st, &c->launches));
@@ -1037,7 +1045,7 @@ int trax_prefix_sum(trax_ctx* c, uint32_t* data, uint64_t n) {
   if (e == cudaSuccess) e = cudaMemsetAsync(c->slots.p, 0, 4, c->st);
   if (e == cudaSuccess)
     e = scan_exclusive(ptr<uint32_t>(tmp), ptr<uint32_t>(tmp), n, nullptr, 0, n, c->scanScratch.p, dev_err(c), c->st,
-                       &c->launches);
+                       &c->launches, false);  // wraps like PrefixSum's uint arithmetic
   if (e == cudaSuccess) e = cudaMemcpyAsync(data, tmp.p, n * 4, cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) rc = cuda_fail(c, e, "trax_prefix_sum");

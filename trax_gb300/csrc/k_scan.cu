@@ -22,9 +22,10 @@ constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __global__ void __launch_bounds__(SCAN_THREADS)
     scan_kernel(const uint32_t* __restrict__ in, uint32_t* out, uint64_t nHost, const uint32_t* nDev,
-                uint32_t nAdd, unsigned long long* status, uint32_t* ticket, uint32_t* err) {
+                uint32_t nAdd, unsigned long long* status, uint32_t* ticket, uint32_t* err, uint32_t overflowBit) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+  __shared__ unsigned long long s_wide[SCAN_THREADS / 32];
   __shared__ uint32_t s_prefix;
   const uint64_t n = nDev ? (uint64_t)(*nDev) + nAdd : nHost;
   if (threadIdx.x == 0) s_tile = atomicAdd(ticket, 1u);
@@ -45,12 +46,16 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     for (int k = 0; k < SCAN_ITEMS; ++k) v[k] = (i0 + k < n) ? in[i0 + k] : 0u;
   }
   uint32_t sum = 0;
+  unsigned long long wide = 0;  // exact thread sum, for the tile aggregate
 #pragma unroll
   for (int k = 0; k < SCAN_ITEMS; ++k) {
     uint32_t t = v[k];
     v[k] = sum;
     sum += t;
+    wide += t;
   }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) wide += __shfl_down_sync(0xffffffffu, wide, d);
   // block-wide exclusive scan of the per-thread sums
   uint32_t incl = sum;
 #pragma unroll
@@ -59,6 +64,7 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     if (lane >= (uint32_t)d) incl += t;
   }
   if (lane == 31) s_warp[warp] = incl;
+  if (lane == 0) s_wide[warp] = wide;
   __syncthreads();
   if (warp == 0) {
     uint32_t w = (lane < SCAN_THREADS / 32) ? s_warp[lane] : 0u;
@@ -69,10 +75,17 @@ __global__ void __launch_bounds__(SCAN_THREADS)
       if (lane >= (uint32_t)d) wi += t;
     }
     if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
-    uint32_t agg = __shfl_sync(0xffffffffu, wi, SCAN_THREADS / 32 - 1);
-    // publish and look back (bounded waits)
-    const uint32_t excl = lb_exclusive_prefix(status, tile, agg, err);
-    if (lane == 0) s_prefix = excl;
+    unsigned long long agg = (lane < SCAN_THREADS / 32) ? s_wide[lane] : 0ull;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) agg += __shfl_down_sync(0xffffffffu, agg, d);
+    agg = __shfl_sync(0xffffffffu, agg, 0);
+    // publish and look back (bounded waits); the 32-bit outputs wrap like the
+    // reference's uint scan, the exact total flags a count past 2^32
+    const unsigned long long excl = lb_exclusive_prefix(status, tile, agg, err);
+    if (lane == 0) {
+      s_prefix = (uint32_t)excl;
+      if (overflowBit && excl + agg > 0xffffffffull) raise_error(err, overflowBit);
+    }
   }
   __syncthreads();
   const uint32_t off = s_prefix + s_warp[warp] + (incl - sum);
@@ -152,7 +165,8 @@ size_t scan_scratch_bytes(uint64_t maxN) {
 }
 
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const uint32_t* nDev, uint32_t nAdd,
-                           uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches) {
+                           uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches,
+                           bool flagOverflow) {
   uint64_t cap = nDev ? maxN : n;
   if (cap == 0) return cudaSuccess;
   uint64_t tiles = (cap + SCAN_TILE - 1) / SCAN_TILE;
@@ -161,7 +175,8 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const 
   if (e != cudaSuccess) return e;
   uint32_t* ticket = reinterpret_cast<uint32_t*>(scratch);
   unsigned long long* status = reinterpret_cast<unsigned long long*>(static_cast<char*>(scratch) + 256);
-  scan_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, out, n, nDev, nAdd, status, ticket, err);
+  scan_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, out, n, nDev, nAdd, status, ticket, err,
+                                                        flagOverflow ? TRAX_EBIT_OVERFLOW : 0u);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }
@@ -258,7 +273,7 @@ extern "C" int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, ui
   e = cudaMemsetAsync(base, 0, NOALLOC_HEADER + tiles * sizeof(unsigned long long), st);
   if (e == cudaSuccess) {
     trax::scan_kernel<<<(unsigned)tiles, trax::SCAN_THREADS, 0, st>>>(d_in, d_out, n, nullptr, 0, status, ticket,
-                                                                      err);
+                                                                      err, 0u);
     e = cudaGetLastError();
   }
   uint32_t hostErr = 0;

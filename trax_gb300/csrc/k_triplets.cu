@@ -131,26 +131,18 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
   if ((threadIdx.x & 31u) == 0 && sent) atomicAdd(sentinels, sent);
 }
 
-// tripletOffsets of predictStore (:404-418); monotonized afterwards
-__global__ void predict_offsets_kernel(DevConfig cfg, const uint32_t* __restrict__ hitEvt,
-                                       const uint32_t* __restrict__ hitLayer, const uint2* __restrict__ pairs,
-                                       const uint32_t* nPairsDev, const uint32_t* candStart, uint32_t* offsets) {
+// tripletOffsets of predictStore (:404-418) + predictOffsetMonotonizeStore
+// (:432-447).  The last non-sentinel pair of a segment stores the candidate
+// position after it, and empty segments inherit their predecessor's value;
+// pairs of a segment are contiguous and sentinel pairs count zero
+// candidates, so both come down to the candidate position at the segment's
+// pair end.
+__global__ void predict_offsets_kernel(uint32_t S, const uint32_t* __restrict__ pairOffsets,
+                                       const uint32_t* __restrict__ nPairsDev, const uint32_t* __restrict__ candStart,
+                                       uint32_t* offsets) {
   const uint32_t nPairs = *nPairsDev;
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < nPairs; g += gridDim.x * blockDim.x) {
-    const uint2 p = pairs[g];
-    if (p.x == TRAX_SENTINEL) continue;
-    const uint32_t event = hitEvt[p.x];
-    const uint32_t lt = hitLayer[p.x] - 1;
-    const uint32_t next = candStart[g + 1];
-    if (g < nPairs - 1) {
-      const uint2 q = pairs[g + 1];
-      const uint32_t nextEvent = q.x == TRAX_SENTINEL ? TRAX_SENTINEL : hitEvt[q.x];
-      const uint32_t nextLT = q.x == TRAX_SENTINEL ? TRAX_SENTINEL : hitLayer[q.x] - 1;
-      if (lt != nextLT || event != nextEvent) offsets[(size_t)event * cfg.nLT + lt + 1] = next;
-    } else {
-      offsets[(size_t)event * cfg.nLT + lt + 1] = next;
-    }
-  }
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= S; s += gridDim.x * blockDim.x)
+    offsets[s] = s == 0 ? 0u : candStart[min(pairOffsets[s], nPairs)];
 }
 
 // filterCount (TripletThetaPhiFilter.h:65-154) for one candidate
@@ -231,20 +223,12 @@ cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid,
   return cudaGetLastError();
 }
 
-cudaError_t predict_offsets(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint32_t* nPairsDev,
-                            uint64_t maxPairs, const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st,
-                            uint32_t* launches) {
+cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, const uint32_t* nPairsDev,
+                            const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st, uint32_t* launches) {
   const uint32_t S = cfg.E * cfg.nLT;
-  cudaError_t e = cudaMemsetAsync(candOffsets, 0, (S + 1) * sizeof(uint32_t), st);
-  if (e != cudaSuccess) return e;
-  if (maxPairs > 0) {
-    predict_offsets_kernel<<<grid_for(maxPairs, 256), 256, 0, st>>>(cfg, hits.evt, hits.layer, pairs, nPairsDev,
-                                                                    candStart, candOffsets);
-    if (launches) *launches += 1;
-  }
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  return max_scan_inclusive(candOffsets, S + 1, st, launches);
+  predict_offsets_kernel<<<grid_for(S + 1, 256), 256, 0, st>>>(S, pairOffsets, nPairsDev, candStart, candOffsets);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
 }
 
 cudaError_t filter_candidates(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint2* cands,

@@ -17,6 +17,7 @@ namespace trax {
 #define TRAX_EBIT_TIMEOUT 1u
 #define TRAX_EBIT_CAPACITY 2u
 #define TRAX_EBIT_BOUNDS 4u
+#define TRAX_EBIT_OVERFLOW 8u  // a count scan's total does not fit in 32 bits
 
 // Everything a kernel needs to know about the workload, passed by value.
 struct DevConfig {

@@ -16,9 +16,11 @@ namespace trax {
 // ---------------------------------------------------------------- scans
 size_t scan_scratch_bytes(uint64_t maxN);
 // Exclusive scan of n elements (or *nDev + nAdd when nDev != nullptr, with
-// maxN bounding the launch), in place allowed.
+// maxN bounding the launch), in place allowed.  Outputs wrap modulo 2^32;
+// with flagOverflow a total of 2^32 or more sets TRAX_EBIT_OVERFLOW.
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const uint32_t* nDev, uint32_t nAdd,
-                           uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches);
+                           uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches,
+                           bool flagOverflow);
 cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* launches);
 
 // ------------------------------------------------------------ grid build
@@ -75,9 +77,8 @@ cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid,
                           const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* keep,
                           uint2* cands, uint64_t capCands, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
                           uint32_t* launches);
-cudaError_t predict_offsets(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint32_t* nPairsDev,
-                            uint64_t maxPairs, const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st,
-                            uint32_t* launches);
+cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, const uint32_t* nPairsDev,
+                            const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st, uint32_t* launches);
 
 // ---------------------------------------------------------------- filter
 cudaError_t filter_candidates(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint2* cands,

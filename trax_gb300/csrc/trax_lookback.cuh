@@ -2,7 +2,8 @@
 // single-pass scan (tiles numbered by an atomic ticket in launch order).
 //
 // Each tile publishes one 64-bit status word: 2 flag bits (0 = nothing yet,
-// 1 = tile aggregate, 2 = inclusive prefix) and a 32-bit value.  Warp 0 of a
+// 1 = tile aggregate, 2 = inclusive prefix) and a 62-bit value, so that sums
+// past 2^32 stay exact and a 32-bit overflow can be detected.  Warp 0 of a
 // tile reads 32 predecessors at a time until it meets an inclusive prefix.
 // The wait for a predecessor is bounded: after TRAX_SPIN_LIMIT polls the tile
 // records TRAX_EBIT_TIMEOUT, counts the missing predecessors as empty and
@@ -16,6 +17,7 @@ namespace trax {
 constexpr unsigned long long LB_FLAG_AGG = 1ull << 62;
 constexpr unsigned long long LB_FLAG_PREFIX = 2ull << 62;
 constexpr unsigned long long LB_FLAG_MASK = 3ull << 62;
+constexpr unsigned long long LB_VALUE_MASK = ~LB_FLAG_MASK;
 
 __device__ __forceinline__ unsigned long long lb_load(const unsigned long long* p) {
   unsigned long long v;
@@ -30,15 +32,16 @@ __device__ __forceinline__ void lb_store(unsigned long long* p, unsigned long lo
 // Called by all 32 lanes of ONE warp with the tile's aggregate; returns (in
 // every lane) the sum of all earlier tiles and publishes this tile's
 // inclusive prefix.
-__device__ __forceinline__ uint32_t lb_exclusive_prefix(unsigned long long* status, uint32_t tile, uint32_t agg,
-                                                        uint32_t* err) {
+__device__ __forceinline__ unsigned long long lb_exclusive_prefix(unsigned long long* status, uint32_t tile,
+                                                                  unsigned long long agg, uint32_t* err) {
   const uint32_t lane = threadIdx.x & 31u;
+  agg &= LB_VALUE_MASK;
   if (tile == 0) {
     if (lane == 0) lb_store(&status[0], LB_FLAG_PREFIX | agg);
-    return 0u;
+    return 0ull;
   }
   if (lane == 0) lb_store(&status[tile], LB_FLAG_AGG | agg);
-  uint32_t excl = 0;
+  unsigned long long excl = 0;
   int64_t pred = (int64_t)tile - 1;
   uint32_t spins = 0;
   while (true) {
@@ -54,12 +57,12 @@ __device__ __forceinline__ uint32_t lb_exclusive_prefix(unsigned long long* stat
       if (flag == 0ull) s = LB_FLAG_AGG;
       flag = s & LB_FLAG_MASK;
     }
-    const uint32_t val = (uint32_t)(s & 0xffffffffull);
+    const unsigned long long val = s & LB_VALUE_MASK;
     const uint32_t pmask = __ballot_sync(0xffffffffu, flag == LB_FLAG_PREFIX);
-    uint32_t contrib = val;
+    unsigned long long contrib = val;
     if (pmask) {
       const uint32_t first = __ffs(pmask) - 1;
-      contrib = (lane <= first) ? val : 0u;
+      contrib = (lane <= first) ? val : 0ull;
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) contrib += __shfl_down_sync(0xffffffffu, contrib, d);
@@ -67,7 +70,7 @@ __device__ __forceinline__ uint32_t lb_exclusive_prefix(unsigned long long* stat
     if (pmask) break;
     pred -= 32;
   }
-  if (lane == 0) lb_store(&status[tile], LB_FLAG_PREFIX | (uint32_t)(excl + agg));
+  if (lane == 0) lb_store(&status[tile], LB_FLAG_PREFIX | ((excl + agg) & LB_VALUE_MASK));
   return excl;
 }
 
