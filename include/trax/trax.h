@@ -247,6 +247,48 @@ int trax_get_tracks(trax_ctx* ctx, uint32_t* states, uint32_t* tracks, uint32_t*
 int trax_get_grid(trax_ctx* ctx, uint32_t* grid, uint64_t* n_cells);
 int trax_get_hit_perm(trax_ctx* ctx, uint32_t* perm);
 
+/* ----------------------------------------------- differentiable alignment
+ * No counterpart in the reference.  An FP32 circle/helix fit of every
+ * selected triplet -- the circle through the three hits (curvature, signed
+ * transverse impact parameter d0; TrackletCircleFitter.h:32-97,
+ * FastCircle.h:41-118) and the least-squares line z = z0 + cot(theta) s in
+ * arc length from the point of closest approach (FastLine.h:15-42) -- with
+ *     chi2 = sum over triplets of d0^2 / sigma_tip^2 + sum_i e_i^2 / sigma_z^2,
+ * e_i the line residuals.  Hits are corrected by per-layer shifts
+ * align[3 l + (0, 1, 2)] = (dr [cm], dz [cm], dphi [rad]) of layer l + 1:
+ * r -> r + dr, phi -> phi + dphi, z -> z + dz.  The per-triplet arithmetic is
+ * FP32; only the sums over triplets are FP64, taken in a fixed order. */
+typedef struct trax_fit_opts {
+  float sigma_z;       /* z resolution of a hit [cm]; <= 0: 0.002 */
+  float sigma_tip[16]; /* per layer triplet [cm]; <= 0: 1.4826 x median |d0| of its rows at zero alignment */
+  int truth_only;      /* 1: only triplets whose three hits share a nonzero hit id */
+} trax_fit_opts;
+
+/* Freezes the fit rows for the current triplets (after trax_triplet_filter,
+ * trax_seed_batch or trax_set_tracklets): triplets whose hits lie on their
+ * layer triplet's layers, optionally truth-matched, with a finite fit at zero
+ * alignment, ordered by layer triplet then event.  The cut decisions are not
+ * revisited by the calls below. */
+int trax_fit_prepare(trax_ctx* ctx, const trax_fit_opts* opts, uint64_t* n_fit);
+/* chi2 at `align` [3 n_layers]; params [n_fit x 4] = (curvature 1/R [1/cm],
+ * d0 [cm], z0 [cm], cot theta) per row when not NULL. */
+int trax_fit_forward(trax_ctx* ctx, const double* align, double* chi2, float* params);
+/* Adjoint kernel: chi2, d chi2 / d align [3 n_layers], an approximate
+ * Gauss-Newton diagonal [3 n_layers] for preconditioning (sum over rows of
+ * (d d0 / d align)^2 / sigma_tip^2 for dr and dphi, of the z residuals'
+ * projector diagonal for dz, and cot(theta)^2 times it for dr) and, when
+ * d_hits is not NULL, d chi2 / d(x, y, z) of every uploaded hit [3 n_hits],
+ * input order.  Any output may be NULL. */
+int trax_fit_backward(trax_ctx* ctx, const double* align, double* chi2, double* d_align, double* gn_diag,
+                      float* d_hits);
+/* Corrects the uploaded hits in place by the shifts `align` [3 n_layers]
+ * (the same transformation as the fit), so that the seeding chain can run
+ * again on the aligned geometry; results of earlier stages are dropped. */
+int trax_apply_alignment(trax_ctx* ctx, const double* align);
+/* Row -> triplet index (into trax_get_triplets' arrays) [n_fit], and the
+ * sigma_tip used per layer triplet [n_lt]. */
+int trax_fit_get_rows(trax_ctx* ctx, uint32_t* triplet_index, float* sigma_tip);
+
 #ifdef __cplusplus
 }
 #endif

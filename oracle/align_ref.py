@@ -17,8 +17,9 @@ adds the alignment model:
   per triplet (P1, P2, P3 corrected):
       circle through the three points: centre C, radius R, curvature 1/R
       transverse impact parameter d0 = |C| - R (signed)
-      point of closest approach to the origin PCA = C d0 / |C|
-      arc lengths s_i = 2 R asin(|P_i - PCA| / 2R)
+      arc lengths from the beam line s_i = 2 R asin(r_i / 2R), r_i = |P_i|
+      (exact for a helix through the beam line; the part of a nonzero d0 that
+      is linear in s is absorbed by the line fit)
       least-squares line Z = z0 + cot(theta) s through the three (s_i, Z_i)
       chi2 = (d0 / sigma_tip)^2 + sum_i e_i^2 / sigma_z^2,  e_i the line residuals
 
@@ -59,11 +60,9 @@ def _forward(X, Y, Z, h1, h2, h3):
     Cn = np.sqrt(Cx * Cx + Cy * Cy)
     num = X1 * X1 + Y1 * Y1 + 2.0 * (X1 * a + Y1 * b)
     d0 = num / (Cn + R)
-    m = d0 / Cn
-    Px, Py = Cx * m, Cy * m
     s, rho, sq = [], [], []
     for (Xi, Yi) in ((X1, Y1), (X2, Y2), (X3, Y3)):
-        r_i = np.hypot(Xi - Px, Yi - Py)
+        r_i = np.hypot(Xi, Yi)
         xi = np.minimum(r_i / (2.0 * R), 1.0)
         s.append(2.0 * R * np.arcsin(xi))
         rho.append(r_i)
@@ -77,7 +76,7 @@ def _forward(X, Y, Z, h1, h2, h3):
     z0 = zb - t * sb
     e = [zi - z0 - t * si for si, zi in zip(s, Zs)]
     return dict(u2=u2, v2=v2, u3=u3, v3=v3, q2=q2, q3=q3, D=D, a=a, b=b, R=R, Cx=Cx, Cy=Cy, Cn=Cn,
-                num=num, d0=d0, m=m, Px=Px, Py=Py, s=s, rho=rho, sq=sq, t=t, z0=z0, e=e,
+                num=num, d0=d0, s=s, rho=rho, sq=sq, t=t, z0=z0, e=e,
                 P=((X1, Y1), (X2, Y2), (X3, Y3)))
 
 
@@ -98,18 +97,11 @@ def loss(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z) -> float:
     return float(np.sum(w * triplet_chi2(x, y, z, layer, h1, h2, h3, align, sigma_tip, sigma_z)))
 
 
-def loss_and_grad(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z):
-    """(loss, dL/dalign [L, 3], dL/d(x, y, z) [H, 3]) by the hand-written adjoint."""
-    x = np.asarray(x, np.float64)
-    y = np.asarray(y, np.float64)
-    z = np.asarray(z, np.float64)
-    align = np.asarray(align, np.float64)
-    lay = np.asarray(layer, np.int64) - 1
-    X, Y, Z = transform(x, y, z, layer, align)
-    f = _forward(X, Y, Z, h1, h2, h3)
-    w = np.asarray(w, np.float64)
-    d0, R, Cn, m = f["d0"], f["R"], f["Cn"], f["m"]
-    L = float(np.sum(w * ((d0 / sigma_tip) ** 2 + sum(ei * ei for ei in f["e"]) / sigma_z ** 2)))
+def _adjoint(f, seed_d0, seed_e):
+    """Reverse pass from d(.)/d d0 = seed_d0 and d(.)/d e_i = seed_e[i] (line
+    parameters held at their least-squares optimum) to the corrected hits:
+    returns ([(gX, gY)] * 3, [gZ] * 3) per triplet slot."""
+    d0, R, Cn = f["d0"], f["R"], f["Cn"]
     t = f["t"]
     gP = [[np.zeros_like(d0), np.zeros_like(d0)] for _ in range(3)]
     gZ = [np.zeros_like(d0) for _ in range(3)]
@@ -117,32 +109,22 @@ def loss_and_grad(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z):
     # s_i at fixed (z0, t)
     g_s = []
     for i in range(3):
-        ge = w * 2.0 * f["e"][i] / sigma_z ** 2
-        gZ[i] = gZ[i] + ge
-        g_s.append(-t * ge)
-    g_d0 = w * 2.0 * d0 / sigma_tip ** 2
+        gZ[i] = gZ[i] + seed_e[i]
+        g_s.append(-t * seed_e[i])
+    g_d0 = seed_d0 + 0.0 * d0
     g_R = np.zeros_like(d0)
-    gPx = np.zeros_like(d0)
-    gPy = np.zeros_like(d0)
     for i in range(3):
         xi = np.minimum(f["rho"][i] / (2.0 * R), 1.0)
-        ds_drho = 1.0 / f["sq"][i]
+        ds_dr = 1.0 / f["sq"][i]
         ds_dR = 2.0 * np.arcsin(xi) - (f["rho"][i] / R) / f["sq"][i]
-        g_rho = g_s[i] * ds_drho
+        g_r = g_s[i] * ds_dr
         g_R = g_R + g_s[i] * ds_dR
         Xi, Yi = f["P"][i]
-        dx, dy = Xi - f["Px"], Yi - f["Py"]
-        gx, gy = g_rho * dx / f["rho"][i], g_rho * dy / f["rho"][i]
-        gP[i][0] = gP[i][0] + gx
-        gP[i][1] = gP[i][1] + gy
-        gPx = gPx - gx
-        gPy = gPy - gy
-    # PCA = C m, m = d0 / Cn
-    g_Cx = gPx * m
-    g_Cy = gPy * m
-    g_m = gPx * f["Cx"] + gPy * f["Cy"]
-    g_d0 = g_d0 + g_m / Cn
-    g_Cn = -g_m * d0 / Cn ** 2
+        gP[i][0] = gP[i][0] + g_r * Xi / f["rho"][i]
+        gP[i][1] = gP[i][1] + g_r * Yi / f["rho"][i]
+    g_Cx = np.zeros_like(d0)
+    g_Cy = np.zeros_like(d0)
+    g_Cn = np.zeros_like(d0)
     # d0 = num / (Cn + R)
     g_num = g_d0 / (Cn + R)
     g_Cn = g_Cn - g_d0 * d0 / (Cn + R)
@@ -189,6 +171,24 @@ def loss_and_grad(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z):
     gP[2][1] = gP[2][1] + g_v3
     gP[0][0] = gP[0][0] - g_u2 - g_u3
     gP[0][1] = gP[0][1] - g_v2 - g_v3
+    return gP, gZ
+
+
+def loss_and_grad(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z, squares=False):
+    """(loss, dL/dalign [L, 3], dL/d(x, y, z) [H, 3]) by the hand-written adjoint;
+    with `squares` also the sum over triplets of each triplet's dchi2/dalign
+    squared [L, 3]."""
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    z = np.asarray(z, np.float64)
+    align = np.asarray(align, np.float64)
+    lay = np.asarray(layer, np.int64) - 1
+    X, Y, Z = transform(x, y, z, layer, align)
+    f = _forward(X, Y, Z, h1, h2, h3)
+    w = np.asarray(w, np.float64)
+    d0 = f["d0"]
+    L = float(np.sum(w * ((d0 / sigma_tip) ** 2 + sum(ei * ei for ei in f["e"]) / sigma_z ** 2)))
+    gP, gZ = _adjoint(f, w * 2.0 * d0 / sigma_tip ** 2, [w * 2.0 * ei / sigma_z ** 2 for ei in f["e"]])
     # corrected-hit gradients -> alignment and raw-hit gradients
     H = x.shape[0]
     gX = np.zeros(H)
@@ -216,7 +216,52 @@ def loss_and_grad(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z):
     g_hits[:, 0] = gX * (fh * c + xr * df_dx) + gY * (fh * s + yr * df_dx)
     g_hits[:, 1] = gX * (-fh * s + xr * df_dy) + gY * (fh * c + yr * df_dy)
     g_hits[:, 2] = gZh
-    return L, g_align, g_hits
+    if not squares:
+        return L, g_align, g_hits
+    g_sq = np.zeros_like(align)
+    for i, h in enumerate((h1, h2, h3)):
+        li = lay[h]
+        per = np.stack([gP[i][0] * dX_ddr[h] + gP[i][1] * dY_ddr[h], gZ[i],
+                        gP[i][0] * dX_ddp[h] + gP[i][1] * dY_ddp[h]], axis=1)
+        for k in range(3):
+            np.add.at(g_sq[:, k], li, per[:, k] ** 2)
+    return L, g_align, g_hits, g_sq
+
+
+def gn_diag(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z):
+    """Approximate Gauss-Newton diagonal [L, 3], a preconditioner: sum over
+    triplets of (d d0/d align)^2 / sigma_tip^2 for dr and dphi, of the z
+    residuals' projector diagonal P_kk = (2/3 - ds_k^2 / S_ss) / sigma_z^2 for
+    dz, and of cot(theta)^2 P_kk for dr (a radial shift slides the hit along
+    its arc; the z residuals' dependence on dphi is left out)."""
+    X, Y, Z = transform(x, y, z, layer, align)
+    f = _forward(X, Y, Z, h1, h2, h3)
+    ones = np.ones_like(f["d0"])
+    zero = np.zeros_like(f["d0"])
+    gP, _ = _adjoint(f, ones, [zero, zero, zero])
+    x = np.asarray(x, np.float64)
+    y = np.asarray(y, np.float64)
+    lay = np.asarray(layer, np.int64) - 1
+    a_h = np.asarray(align, np.float64)[lay]
+    dr, dp = a_h[:, 0], a_h[:, 2]
+    r = np.hypot(x, y)
+    fh = (r + dr) / r
+    c, s_ = np.cos(dp), np.sin(dp)
+    xr, yr = x * c - y * s_, x * s_ + y * c
+    sb = (f["s"][0] + f["s"][1] + f["s"][2]) / 3.0
+    Sss = sum((si - sb) ** 2 for si in f["s"])
+    out = np.zeros((np.asarray(align).shape[0], 3))
+    wt = np.asarray(w, np.float64) / np.asarray(sigma_tip, np.float64) ** 2
+    for i, h in enumerate((h1, h2, h3)):
+        ddr = (gP[i][0] * xr[h] + gP[i][1] * yr[h]) / r[h]
+        ddp = fh[h] * (gP[i][1] * xr[h] - gP[i][0] * yr[h])
+        np.add.at(out[:, 0], lay[h], wt * ddr ** 2)
+        np.add.at(out[:, 2], lay[h], wt * ddp ** 2)
+        proj = np.asarray(w, np.float64) * (2.0 / 3.0 - (f["s"][i] - sb) ** 2 / Sss) / sigma_z ** 2
+        np.add.at(out[:, 1], lay[h], proj)
+        # a radial shift moves the hit along its arc: ds = dr / sq, de ~ -cot(theta) ds
+        np.add.at(out[:, 0], lay[h], proj * (f["t"] / f["sq"][i]) ** 2)
+    return out
 
 
 def fd_grad_align(x, y, z, layer, h1, h2, h3, w, align, sigma_tip, sigma_z, h=1e-6):

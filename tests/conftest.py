@@ -25,3 +25,9 @@ def trax_lib():
     from trax_gb300 import build, capi
     build.build()
     return capi
+
+
+@pytest.fixture(scope="session")
+def align_ref():
+    from oracle import align_ref as a
+    return a

@@ -29,7 +29,8 @@ EXPORTED = [
     "trax_cellular_automaton", "trax_prefix_sum", "trax_seed_batch", "trax_get_stats", "trax_get_pairs",
     "trax_get_timings", "trax_get_candidates", "trax_get_triplets", "trax_get_triplet_eta_pt", "trax_get_links",
     "trax_get_tracks", "trax_get_grid", "trax_get_hit_perm", "trax_set_block_sizes", "trax_get_launch_config",
-    "trax_autotune",
+    "trax_autotune", "trax_fit_prepare", "trax_fit_forward", "trax_fit_backward", "trax_fit_get_rows",
+    "trax_apply_alignment",
 ]
 
 
@@ -62,6 +63,10 @@ class BatchStatsC(ctypes.Structure):
         "n_hits", "n_pairs", "n_candidates", "n_triplets", "n_links", "n_connectable", "n_non_connectable",
         "n_track_entries", "n_pair_sentinels", "n_candidate_sentinels", "kernel_launches")] + [
         ("device_ms", ctypes.c_double)]
+
+
+class FitOptsC(ctypes.Structure):
+    _fields_ = [("sigma_z", ctypes.c_float), ("sigma_tip", ctypes.c_float * 16), ("truth_only", ctypes.c_int)]
 
 
 class TuneOptsC(ctypes.Structure):
@@ -126,6 +131,11 @@ def load() -> ctypes.CDLL:
             "trax_set_block_sizes": ([vp, u32, u32, u32], i32),
             "trax_get_launch_config": ([vp, vp], i32),
             "trax_autotune": ([vp, ctypes.c_char_p, vp, vp], i32),
+            "trax_fit_prepare": ([vp, vp, pu64], i32),
+            "trax_fit_forward": ([vp, vp, vp, vp], i32),
+            "trax_fit_backward": ([vp, vp, vp, vp, vp, vp], i32),
+            "trax_fit_get_rows": ([vp, vp, vp], i32),
+            "trax_apply_alignment": ([vp, vp], i32),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -172,6 +182,7 @@ class Context:
         self.n_hits = 0
         self.n_z = 0
         self.n_phi = 0
+        self.n_fit = 0
 
     # ------------------------------------------------------------ plumbing
     def _check(self, rc: int):
@@ -289,6 +300,51 @@ class Context:
         out = {f[0]: getattr(res, f[0]) for f in TuneResultC._fields_}
         self.n_z, self.n_phi = out["n_z"], out["n_phi"]
         return out
+
+    # ------------------------------------------------ differentiable fit
+    def fit_prepare(self, sigma_z: float = 0.0, sigma_tip=None, truth_only: bool = False) -> int:
+        """trax_fit_prepare: freeze the fit rows of the current triplets; returns their number."""
+        o = FitOptsC()
+        o.sigma_z = sigma_z
+        for k, v in enumerate(sigma_tip or []):
+            o.sigma_tip[k] = v
+        o.truth_only = int(truth_only)
+        n = ctypes.c_uint64()
+        self._check(self._L.trax_fit_prepare(self._h, ctypes.byref(o), ctypes.byref(n)))
+        self.n_fit = int(n.value)
+        return self.n_fit
+
+    def fit_forward(self, align: np.ndarray, params: bool = False):
+        """(chi2, params [n_fit, 4] or None) at align [n_layers, 3] = (dr, dz, dphi)."""
+        a = np.ascontiguousarray(align, dtype=np.float64).ravel()
+        chi2 = ctypes.c_double()
+        p = np.zeros((max(self.n_fit, 1), 4), dtype=np.float32) if params else None
+        self._check(self._L.trax_fit_forward(self._h, _p(a), ctypes.byref(chi2), _p(p)))
+        return chi2.value, (p[:self.n_fit] if params else None)
+
+    def fit_backward(self, align: np.ndarray, hits: bool = False, squares: bool = False):
+        """(chi2, d chi2/d align [n_layers, 3], d chi2/d hits [n_hits, 3] or None), plus the
+        approximate Gauss-Newton diagonal [n_layers, 3] when `squares`."""
+        a = np.ascontiguousarray(align, dtype=np.float64).ravel()
+        chi2 = ctypes.c_double()
+        g = np.zeros_like(a)
+        g2 = np.zeros_like(a) if squares else None
+        gh = np.zeros((max(self.n_hits, 1), 3), dtype=np.float32) if hits else None
+        self._check(self._L.trax_fit_backward(self._h, _p(a), ctypes.byref(chi2), _p(g), _p(g2), _p(gh)))
+        out = (chi2.value, g.reshape(-1, 3), (gh[:self.n_hits] if hits else None))
+        return out + (g2.reshape(-1, 3),) if squares else out
+
+    def apply_alignment(self, align: np.ndarray):
+        """trax_apply_alignment: correct the uploaded hits in place (rerun the chain afterwards)."""
+        a = np.ascontiguousarray(align, dtype=np.float64).ravel()
+        self._check(self._L.trax_apply_alignment(self._h, _p(a)))
+
+    def fit_rows(self):
+        """(triplet index of every fit row, sigma_tip per layer triplet)."""
+        r = np.zeros(max(self.n_fit, 1), dtype=np.uint32)
+        s = np.zeros(16, dtype=np.float32)
+        self._check(self._L.trax_fit_get_rows(self._h, _p(r), _p(s)))
+        return r[:self.n_fit], s[:self.n_lt]
 
     def stats(self) -> BatchStats:
         st = BatchStatsC()

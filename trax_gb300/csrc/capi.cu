@@ -139,7 +139,15 @@ struct trax_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double lastMs = 0.0;
   // per-stage and per-kernel timing events of the last run
+  // differentiable fit: rows frozen by trax_fit_prepare for one triplet set
+  DevBuf fitOk, fitSegCnt, fitSegDelta, fitRows, fitPartials, fitOut, fitParams, fitDHits, fitDHitsF;
+  FitConfig fitCfg;
+  uint64_t nFit = 0;
+  bool fitReady = false;
+  uint64_t tripGen = 1, fitTripGen = 0;  // generation of the triplet set
+  float fitSigmaTip[TRAX_MAX_LT] = {};
   cudaEvent_t stageEv[N_STAGES + 1] = {};
+
   cudaEvent_t kEv[2 * TK_N] = {};
   bool stageUsed[N_STAGES] = {};
   bool kUsed[TK_N] = {};
@@ -639,6 +647,7 @@ int run_stage(trax_ctx* c, int stage) {
   c->stageUsed[stage - 1] = true;
   RC(check_device_error(c));
   c->stage = stage;
+  if (stage == 4) ++c->tripGen;
   return TRAX_OK;
 }
 
@@ -774,6 +783,61 @@ int copy_out(trax_ctx* c, void* dst, const DevBuf& src, size_t bytes) {
   return TRAX_OK;
 }
 
+// ------------------------------------------------------- differentiable fit
+// per-layer corrections from double-precision shifts (dr, dz, dphi)
+int fit_set_alignment(trax_ctx* c, const double* align) {
+  FitConfig& f = c->fitCfg;
+  for (uint32_t l = 0; l < TRAX_MAX_LAYERS; ++l) f.dr[l] = f.dz[l] = f.sn[l] = f.cm1[l] = 0.0f;
+  if (!align) return TRAX_OK;
+  for (uint32_t l = 0; l < c->L; ++l) {
+    const double dr = align[3 * l], dz = align[3 * l + 1], dp = align[3 * l + 2];
+    if (!std::isfinite(dr) || !std::isfinite(dz) || !std::isfinite(dp))
+      return fail(c, TRAX_ERR_ARG, "alignment parameters must be finite");
+    const double h = std::sin(0.5 * dp);
+    f.dr[l] = (float)dr;
+    f.dz[l] = (float)dz;
+    f.sn[l] = (float)std::sin(dp);
+    f.cm1[l] = (float)(-2.0 * h * h);  // cos(dphi) - 1 without cancellation
+  }
+  return TRAX_OK;
+}
+
+TripletView fit_triplets(trax_ctx* c) {
+  TripletView t;
+  t.h1 = ptr<uint32_t>(c->h1);
+  t.h2 = ptr<uint32_t>(c->h2);
+  t.h3 = ptr<uint32_t>(c->h3);
+  t.nDev = nullptr;
+  t.maxN = c->nT;
+  return t;
+}
+
+int fit_check(trax_ctx* c) {
+  if (!c->fitReady || c->fitTripGen != c->tripGen || c->stage < 4)
+    return fail(c, TRAX_ERR_STATE, "trax_fit_prepare must run on the current triplets first");
+  return TRAX_OK;
+}
+
+// chi2 and gradients at `align` into fitOut (1 + 3 L doubles); optional
+// per-row parameters and grid-order hit gradients
+int fit_run(trax_ctx* c, const double* align, bool grad, bool params, bool hitsGrad) {
+  RC(fit_set_alignment(c, align));
+  const FitConfig& f = c->fitCfg;
+  CK(ensure(c, c->fitPartials, (size_t)std::max<uint32_t>(f.nBlocks, 1) * TRAX_FIT_SLOTS * sizeof(double)));
+  CK(ensure(c, c->fitOut, (1 + 6 * (size_t)c->L) * sizeof(double)));
+  if (params) CK(ensure(c, c->fitParams, std::max<uint64_t>(c->nFit, 1) * 16));
+  double* dH = nullptr;
+  if (hitsGrad) {
+    CK(ensure(c, c->fitDHits, std::max<uint64_t>(c->nHits, 1) * 3 * sizeof(double)));
+    CK(cudaMemsetAsync(c->fitDHits.p, 0, (size_t)c->nHits * 3 * sizeof(double), c->st));
+    dH = ptr<double>(c->fitDHits);
+  }
+  CK(fit_eval(f, grad, dev_hits(c), fit_triplets(c), ptr<uint32_t>(c->fitRows), ptr<double>(c->fitPartials),
+              params ? ptr<float>(c->fitParams) : nullptr, dH, c->st, &c->launches));
+  CK(fit_reduce(f, ptr<double>(c->fitPartials), ptr<double>(c->fitOut), c->st, &c->launches));
+  return TRAX_OK;
+}
+
 }  // namespace
 
 // ======================================================================= C ABI
@@ -816,7 +880,9 @@ void trax_destroy(trax_ctx* c) {
                     &c->candOffsets, &c->flags, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,
-                    &c->isBest, &c->handlers, &c->tracks, &c->scanScratch, &c->slots};
+                    &c->isBest, &c->handlers, &c->tracks, &c->scanScratch, &c->slots, &c->fitOk, &c->fitSegCnt,
+                    &c->fitSegDelta, &c->fitRows, &c->fitPartials, &c->fitOut, &c->fitParams, &c->fitDHits,
+                    &c->fitDHitsF};
   for (DevBuf* b : bufs) release(*b);
   if (c->hSlots) cudaFreeHost(c->hSlots);
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -991,6 +1057,7 @@ int trax_set_tracklets(trax_ctx* c, const uint32_t* h1, const uint32_t* h2, cons
   c->identityHits = true;
   RC(check_device_error(c));
   c->stage = 4;
+  ++c->tripGen;
   return TRAX_OK;
 }
 
@@ -1125,6 +1192,7 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
     }
     RC(error_from_bits(c, bits));
     c->stage = linking ? 7 : 4;
+    ++c->tripGen;
     fill_stats(c, stats);
     return TRAX_OK;
   }
@@ -1229,6 +1297,175 @@ int trax_get_hit_perm(trax_ctx* c, uint32_t* perm) {
   if (!c) return TRAX_ERR_ARG;
   if (c->stage < 1) return fail(c, TRAX_ERR_STATE, "grid not built");
   RC(copy_out(c, perm, c->porig, (size_t)c->nHits * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+// ------------------------------------------------------- differentiable fit
+int trax_fit_prepare(trax_ctx* c, const trax_fit_opts* opts, uint64_t* n_fit) {
+  if (!c) return TRAX_ERR_ARG;
+  if (c->stage < 4) return fail(c, TRAX_ERR_STATE, "triplets not filtered");
+  CK(cudaSetDevice(c->device));
+  c->fitReady = false;
+  const float sigmaZ = (opts && opts->sigma_z > 0.0f) ? opts->sigma_z : 0.002f;
+  const int truthOnly = opts ? opts->truth_only : 0;
+  FitConfig& f = c->fitCfg;
+  memset(&f, 0, sizeof(f));
+  f.L = c->L;
+  f.nLT = (uint32_t)c->lts.size();
+  for (uint32_t k = 0; k < f.nLT; ++k) {
+    f.layer[0][k] = c->lts[k].layer1 - 1;
+    f.layer[1][k] = c->lts[k].layer2 - 1;
+    f.layer[2][k] = c->lts[k].layer3 - 1;
+    f.wTip[k] = 1.0f;
+  }
+  f.wZ = 1.0f / (sigmaZ * sigmaZ);
+  RC(fit_set_alignment(c, nullptr));
+  const uint64_t nT = c->nT;
+  const uint32_t S = c->E * f.nLT;
+  // 1. selection flags and per-segment counts
+  CK(ensure(c, c->fitOk, (nT + 1) * 4));
+  CK(ensure(c, c->fitSegCnt, (size_t)S * 4));
+  CK(ensure(c, c->fitSegDelta, (size_t)S * 4));
+  CK(cudaMemsetAsync(c->fitSegCnt.p, 0, (size_t)S * 4, c->st));
+  uint32_t* ok = ptr<uint32_t>(c->fitOk);
+  CK(fit_select(f, c->cfg, dev_hits(c), fit_triplets(c), nT, truthOnly, ok, ptr<uint32_t>(c->fitSegCnt), c->st,
+                &c->launches));
+  CK(ensure(c, c->scanScratch, scan_scratch_bytes(nT + 1)));
+  CK(scan_exclusive(ok, ok, nT + 1, nullptr, 0, nT + 1, c->scanScratch.p, dev_err(c), c->st, &c->launches, true));
+  // 2. rows ordered by layer triplet, then by event (segment order inside a layer triplet)
+  std::vector<uint32_t> cnt(S);
+  if (S) CK(cudaMemcpyAsync(cnt.data(), c->fitSegCnt.p, (size_t)S * 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  RC(check_device_error(c));
+  std::vector<uint64_t> cStart(S), ltCount(f.nLT, 0);
+  uint64_t run = 0;
+  for (uint32_t s = 0; s < S; ++s) {
+    cStart[s] = run;
+    run += cnt[s];
+    ltCount[s % f.nLT] += cnt[s];
+  }
+  if (run > 0xffffffffull) return fail(c, TRAX_ERR_CAPACITY, "too many fit rows");
+  c->nFit = run;
+  uint64_t base = 0, blk = 0;
+  for (uint32_t k = 0; k < f.nLT; ++k) {
+    f.ltBase[k] = (uint32_t)base;
+    f.blkStart[k] = (uint32_t)blk;
+    base += ltCount[k];
+    blk += (ltCount[k] + TRAX_FIT_CHUNK - 1) / TRAX_FIT_CHUNK;
+  }
+  f.ltBase[f.nLT] = (uint32_t)base;
+  f.blkStart[f.nLT] = (uint32_t)blk;
+  f.nBlocks = (uint32_t)blk;
+  std::vector<int32_t> delta(S);
+  std::vector<uint64_t> inLT(f.nLT, 0);
+  for (uint32_t s = 0; s < S; ++s) {
+    const uint32_t k = s % f.nLT;
+    delta[s] = (int32_t)((int64_t)(f.ltBase[k] + inLT[k]) - (int64_t)cStart[s]);
+    inLT[k] += cnt[s];
+  }
+  if (S) CK(cudaMemcpyAsync(c->fitSegDelta.p, delta.data(), (size_t)S * 4, cudaMemcpyHostToDevice, c->st));
+  CK(ensure(c, c->fitRows, std::max<uint64_t>(c->nFit, 1) * 4));
+  CK(fit_scatter(c->cfg, dev_hits(c), fit_triplets(c), nT, ok, ptr<int32_t>(c->fitSegDelta),
+                 ptr<uint32_t>(c->fitRows), c->st, &c->launches));
+  // 3. sigma_tip per layer triplet: given, or 1.4826 x median |d0| at zero alignment
+  bool needD0 = false;
+  for (uint32_t k = 0; k < f.nLT; ++k) {
+    const float g = opts ? opts->sigma_tip[k] : 0.0f;
+    c->fitSigmaTip[k] = g;
+    needD0 = needD0 || !(g > 0.0f);
+  }
+  if (needD0 && c->nFit) {
+    c->fitReady = true;
+    c->fitTripGen = c->tripGen;
+    RC(fit_run(c, nullptr, false, true, false));
+    std::vector<float> prm(c->nFit * 4);
+    CK(cudaMemcpyAsync(prm.data(), c->fitParams.p, c->nFit * 16, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->fitReady = false;
+    for (uint32_t k = 0; k < f.nLT; ++k) {
+      if (c->fitSigmaTip[k] > 0.0f) continue;
+      std::vector<float> a;
+      for (uint32_t r = f.ltBase[k]; r < f.ltBase[k + 1]; ++r) a.push_back(std::fabs(prm[4 * (size_t)r + 1]));
+      float sig = 1.0f;
+      if (!a.empty()) {
+        std::nth_element(a.begin(), a.begin() + a.size() / 2, a.end());
+        sig = 1.4826f * a[a.size() / 2];
+        if (!(sig > 0.0f)) sig = 1e-4f;
+      }
+      c->fitSigmaTip[k] = sig;
+    }
+  }
+  for (uint32_t k = 0; k < f.nLT; ++k) {
+    const float sg = c->fitSigmaTip[k] > 0.0f ? c->fitSigmaTip[k] : 1.0f;
+    c->fitSigmaTip[k] = sg;
+    f.wTip[k] = 1.0f / (sg * sg);
+  }
+  c->fitReady = true;
+  c->fitTripGen = c->tripGen;
+  if (n_fit) *n_fit = c->nFit;
+  return TRAX_OK;
+}
+
+int trax_fit_forward(trax_ctx* c, const double* align, double* chi2, float* params) {
+  if (!c || !align) return TRAX_ERR_ARG;
+  RC(fit_check(c));
+  CK(cudaSetDevice(c->device));
+  RC(fit_run(c, align, false, params != nullptr, false));
+  double out = 0.0;
+  CK(cudaMemcpyAsync(&out, c->fitOut.p, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  if (params && c->nFit) CK(cudaMemcpyAsync(params, c->fitParams.p, c->nFit * 16, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (chi2) *chi2 = out;
+  return TRAX_OK;
+}
+
+int trax_fit_backward(trax_ctx* c, const double* align, double* chi2, double* d_align, double* gn_diag,
+                      float* d_hits) {
+  if (!c || !align) return TRAX_ERR_ARG;
+  RC(fit_check(c));
+  CK(cudaSetDevice(c->device));
+  RC(fit_run(c, align, true, false, d_hits != nullptr));
+  std::vector<double> out(1 + 6 * (size_t)c->L);
+  CK(cudaMemcpyAsync(out.data(), c->fitOut.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  if (d_hits && c->nHits) {
+    CK(ensure(c, c->fitDHitsF, (size_t)c->nHits * 3 * sizeof(float)));
+    CK(fit_hits_out(ptr<double>(c->fitDHits), ptr<uint32_t>(c->porig), c->nHits, ptr<float>(c->fitDHitsF), c->st,
+                    &c->launches));
+    CK(cudaMemcpyAsync(d_hits, c->fitDHitsF.p, (size_t)c->nHits * 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                       c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  if (chi2) *chi2 = out[0];
+  if (d_align)
+    for (size_t k = 0; k < 3 * (size_t)c->L; ++k) d_align[k] = out[1 + k];
+  if (gn_diag)
+    for (size_t k = 0; k < 3 * (size_t)c->L; ++k) gn_diag[k] = out[1 + 3 * (size_t)c->L + k];
+  return TRAX_OK;
+}
+
+int trax_apply_alignment(trax_ctx* c, const double* align) {
+  if (!c || !align) return TRAX_ERR_ARG;
+  if (!c->haveHits) return fail(c, TRAX_ERR_STATE, "no hits uploaded");
+  CK(cudaSetDevice(c->device));
+  c->fitCfg.L = c->L;
+  RC(fit_set_alignment(c, align));
+  CK(fit_apply(c->fitCfg, ptr<float>(c->in_x), ptr<float>(c->in_y), ptr<float>(c->in_z), ptr<uint32_t>(c->in_layer),
+               c->nHits, c->st, &c->launches));
+  CK(cudaStreamSynchronize(c->st));
+  c->stage = 0;  // every stage output refers to the old positions
+  c->fitReady = false;
+  ++c->tripGen;
+  drop_graph(c);
+  return TRAX_OK;
+}
+
+int trax_fit_get_rows(trax_ctx* c, uint32_t* triplet_index, float* sigma_tip) {
+  if (!c) return TRAX_ERR_ARG;
+  RC(fit_check(c));
+  if (triplet_index && c->nFit) RC(copy_out(c, triplet_index, c->fitRows, c->nFit * 4));
+  if (sigma_tip)
+    for (size_t k = 0; k < c->lts.size(); ++k) sigma_tip[k] = c->fitSigmaTip[k];
   CK(cudaStreamSynchronize(c->st));
   return TRAX_OK;
 }

@@ -144,6 +144,53 @@ cudaError_t ca_backward(const uint32_t* basis, const float* pt, CABuffers b, con
 cudaError_t ca_tracks(CABuffers b, const uint32_t* nTDev, uint64_t maxT, uint32_t* tracks, uint64_t maxTracks,
                       uint32_t* err, cudaStream_t st, uint32_t* launches);
 
+// ------------------------------------------- differentiable triplet fit
+// Fit rows are the selected triplets ordered by layer triplet; rows of layer
+// triplet k are [ltBase[k], ltBase[k+1]) and are reduced by the blocks
+// [blkStart[k], blkStart[k+1]), each taking FIT_CHUNK rows, so that every
+// FP64 sum is taken in a fixed order.
+#define TRAX_FIT_CHUNK 4096u
+// per block: chi2, d chi2 / d(dr, dz, dphi) of the three hit layers, and an
+// approximate Gauss-Newton diagonal for the same nine (a preconditioner)
+#define TRAX_FIT_SLOTS 19
+
+struct FitConfig {
+  uint32_t L, nLT, nBlocks;
+  uint32_t layer[3][TRAX_MAX_LT];  // 0-based layer of each hit slot of a layer triplet
+  float wTip[TRAX_MAX_LT];         // 1 / sigma_tip^2 per layer triplet
+  float wZ;                        // 1 / sigma_z^2
+  // per-layer correction: r -> r + dr, z -> z + dz, rotation by dphi given
+  // as sin(dphi) and cos(dphi) - 1 (both from double precision on the host)
+  float dr[TRAX_MAX_LAYERS], dz[TRAX_MAX_LAYERS], sn[TRAX_MAX_LAYERS], cm1[TRAX_MAX_LAYERS];
+  uint32_t ltBase[TRAX_MAX_LT + 1];
+  uint32_t blkStart[TRAX_MAX_LT + 1];
+};
+
+// ok[t] = 1 for triplets whose hits lie on their layer triplet's layers, whose
+// three hits share a nonzero hit id when truthOnly, and whose fit at the
+// configured alignment is finite; segCount[s] counts them per segment
+cudaError_t fit_select(const FitConfig& fc, const DevConfig& cfg, DevHits hits, TripletView t, uint64_t nT,
+                       int truthOnly, uint32_t* ok, uint32_t* segCount, cudaStream_t st, uint32_t* launches);
+// rows[okScan[t] + segDelta[seg(t)]] = t for the selected triplets
+cudaError_t fit_scatter(const DevConfig& cfg, DevHits hits, TripletView t, uint64_t nT, const uint32_t* okScan,
+                        const int32_t* segDelta, uint32_t* rows, cudaStream_t st, uint32_t* launches);
+// chi2 (and with grad: alignment and hit gradients) of the fit rows.
+// partials[b * TRAX_FIT_SLOTS + k]; params[row * 4] = (curvature, d0, z0,
+// cot theta) when not null; dHits (double, grid order, 3 per hit) is added to
+// when not null.
+cudaError_t fit_eval(const FitConfig& fc, bool grad, DevHits hits, TripletView t, const uint32_t* rows,
+                     double* partials, float* params, double* dHits, cudaStream_t st, uint32_t* launches);
+// out[0] = chi2, out[1 + 3 l + p] = d chi2 / d(dr, dz, dphi)_l, and
+// out[1 + 3 L + 3 l + p] = the approximate Gauss-Newton diagonal; fixed-order sums
+cudaError_t fit_reduce(const FitConfig& fc, const double* partials, double* out, cudaStream_t st,
+                       uint32_t* launches);
+// uploaded (input-order) hits corrected in place by fc's per-layer shifts
+cudaError_t fit_apply(const FitConfig& fc, float* x, float* y, float* z, const uint32_t* layer, uint64_t n,
+                      cudaStream_t st, uint32_t* launches);
+// float gradient per input hit from the double grid-order sums
+cudaError_t fit_hits_out(const double* dHits, const uint32_t* orig, uint64_t nHits, float* out, cudaStream_t st,
+                         uint32_t* launches);
+
 // number of SMs of the current device (cached)
 int sm_count();
 

@@ -131,8 +131,12 @@ def workload(config: int, n_events: Optional[int] = None) -> Workload:
                      n_tracks=200, pt_dist="exp", pt_range=(0.5, 0.0), eta_max=1.5,
                      noise_fraction=0.2)
     elif config in (2, 4):
+        # the alignment workload adds the layer triplets (7,8,9) and (8,9,10):
+        # with only the first six, layers 9 and 10 are in no triplet and
+        # their shifts have no gradient
         w = Workload("ttbarlike-1000-uneven-10layer" if config == 2 else "alignment-1000-10layer",
-                     config, 1000, BARREL10_RADII, layer_triplets([1, 2, 3, 4, 5, 6]),
+                     config, 1000, BARREL10_RADII,
+                     layer_triplets([1, 2, 3, 4, 5, 6] if config == 2 else [1, 2, 3, 4, 5, 6, 7, 8]),
                      50, 128, 0.7, tracks="poisson_uniform_lambda", pt_dist="powerlaw3",
                      pt_range=(0.7, 0.0), eta_max=2.5, misalign=(config == 4))
     elif config == 3:
@@ -142,6 +146,14 @@ def workload(config: int, n_events: Optional[int] = None) -> Workload:
                      noise_fraction=0.05)
     else:
         raise ValueError(f"unknown config {config}")
+    if config == 4:
+        # A radial shift moves a track's predicted z on the next layer by
+        # cot(theta) * dr (up to 0.03 cm for 50 um at |eta| = 2.5), close to
+        # the prediction window's sigma_z = 0.037 cm: windows that tight keep
+        # triplets by their misalignment-made z residual and bias the fitted
+        # shifts by several um.  The alignment workload opens the z windows
+        # four times.
+        w = dataclasses.replace(w, lts=[dataclasses.replace(lt, sigma_z=4.0 * lt.sigma_z) for lt in w.lts])
     if n_events is not None:
         w = dataclasses.replace(w, n_events=int(n_events))
     return w
@@ -205,8 +217,12 @@ class EventBatch:
                 parts[k].append(v)
             lh.append(self.layer_hits[e])
         layer_hits = np.array(lh, dtype=np.uint32).reshape(len(events), self.n_layers)
-        return _assemble({k: np.concatenate(v) if v else np.zeros(0, np.uint32) for k, v in parts.items()},
-                         layer_hits, self)
+        out = _assemble({k: np.concatenate(v) if v else np.zeros(0, np.uint32) for k, v in parts.items()},
+                        layer_hits, self)
+        out.misalignment = self.misalignment
+        if self.track_pt is not None:
+            out.track_pt = [self.track_pt[e] for e in events]
+        return out
 
 
 def _assemble(cols, layer_hits, like: "EventBatch") -> "EventBatch":
