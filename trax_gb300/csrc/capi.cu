@@ -101,6 +101,7 @@ struct trax_ctx {
   uint32_t nZ = 0, nP = 0;
   uint32_t pairThreads = 128, predThreads = 128, filterThreads = 256;  // launch shape
   bool haveLT = false, haveGeom = false, haveGrid = false, haveHits = false;
+  bool cfgDirty = true;  // layer triplets or geometry changed since the device configuration was built
   // batch shape
   uint32_t E = 0, L = 0, nHits = 0;
   float dEtaCut = 0.0256f;
@@ -248,8 +249,12 @@ float min_radius_curvature(float minPt) {
   return (float)(minPt * GEV_C / (IDEAL_BZ * Q) * 1E2);
 }
 
-int build_config(trax_ctx* c) {
-  if (!c->haveLT || !c->haveGeom || !c->haveGrid || !c->haveHits)
+// Device configuration from the host-side settings.  The grid build needs
+// only the grid and the hits; the seeding stages (`seeding`) also need the
+// layer triplets and the geometry.
+int build_config(trax_ctx* c, bool seeding = true) {
+  if (!c->haveGrid || !c->haveHits) return fail(c, TRAX_ERR_STATE, "grid and hits must be set first");
+  if (seeding && (!c->haveLT || !c->haveGeom))
     return fail(c, TRAX_ERR_STATE, "layer triplets, geometry, grid and hits must be set first");
   DevConfig& g = c->cfg;
   memset(&g, 0, sizeof(g));
@@ -258,7 +263,7 @@ int build_config(trax_ctx* c) {
   g.nZ = c->nZ;
   g.nP = c->nP;
   g.C = (c->nZ + 1) * (c->nP + 1);
-  g.nLT = (uint32_t)c->lts.size();
+  g.nLT = c->haveLT ? (uint32_t)c->lts.size() : 0u;
   // Grid.h:9-15, 33-37 (float arithmetic on the host)
   const float MIN_Z = -300.0f, MAX_Z = 300.0f;
   const float MIN_PHI = (float)-3.14159265358979323846, MAX_PHI = (float)3.14159265358979323846;
@@ -288,6 +293,8 @@ int build_config(trax_ctx* c) {
     memcpy(&sp, &t.pair_spread_phi, 4);
     g.pairSigmaPhi[p] = sp;
   }
+  c->cfgDirty = !(c->haveLT && c->haveGeom);
+  if (!c->haveGeom) return TRAX_OK;
   if (c->minR.size() < c->L) return fail(c, TRAX_ERR_ARG, "geometry has fewer layers than the hits");
   const float twoR = 2 * g.minRcurv;
   for (uint32_t l = 0; l < c->L; ++l) {
@@ -615,8 +622,8 @@ int stage_ca(trax_ctx* c, Mode mode) {
   return TRAX_OK;
 }
 
-int begin_run(trax_ctx* c) {
-  RC(build_config(c));
+int begin_run(trax_ctx* c, bool seeding) {
+  RC(build_config(c, seeding));
   c->sortedSegments = true;
   c->identityHits = false;
   CK(cudaSetDevice(c->device));
@@ -626,6 +633,7 @@ int begin_run(trax_ctx* c) {
 
 int run_stage(trax_ctx* c, int stage) {
   if (stage > 1 && c->stage < stage - 1) return fail(c, TRAX_ERR_STATE, "the previous stage has not run");
+  if (stage > 1 && c->cfgDirty) RC(build_config(c, true));  // layer triplets or geometry set after the grid
   int rc = TRAX_OK;
   if (stage == 1) {
     for (bool& u : c->stageUsed) u = false;
@@ -633,7 +641,7 @@ int run_stage(trax_ctx* c, int stage) {
   }
   cudaEventRecord(c->stageEv[stage - 1], c->st);
   switch (stage) {
-    case 1: rc = begin_run(c); if (!rc) rc = stage_grid(c, SYNCED); break;
+    case 1: rc = begin_run(c, false); if (!rc) rc = stage_grid(c, SYNCED); break;
     case 2: rc = stage_pairs(c, SYNCED); break;
     case 3: rc = stage_predict(c, SYNCED); break;
     case 4: rc = stage_filter(c, SYNCED); break;
@@ -910,7 +918,8 @@ int trax_set_layer_triplets(trax_ctx* c, const trax_layer_triplet* lt, int n, fl
   c->lts.assign(lt, lt + n);
   c->minPt = min_pt;
   c->haveLT = true;
-  c->stage = 0;
+  c->stage = c->identityHits ? 0 : std::min(c->stage, 1);  // a built grid stays valid
+  c->cfgDirty = true;
   return TRAX_OK;
 }
 
@@ -920,7 +929,8 @@ int trax_set_geometry(trax_ctx* c, const float* min_r, const float* max_r, int n
   c->minR.assign(min_r, min_r + n_layers);
   c->maxR.assign(max_r, max_r + n_layers);
   c->haveGeom = true;
-  c->stage = 0;
+  c->stage = c->identityHits ? 0 : std::min(c->stage, 1);  // a built grid stays valid
+  c->cfgDirty = true;
   return TRAX_OK;
 }
 
@@ -1003,7 +1013,7 @@ int trax_grid_build(trax_ctx* c) { return c ? run_stage(c, 1) : TRAX_ERR_ARG; }
 
 int trax_set_tracklets(trax_ctx* c, const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, uint64_t n) {
   if (!c || (n && (!h1 || !h2 || !h3))) return fail(c, TRAX_ERR_ARG, "null triplet columns");
-  RC(begin_run(c));
+  RC(begin_run(c, true));
   const Mode mode = SYNCED;
   const uint64_t nh = c->nHits;
   if (n > 0xfffffff0ull) return fail(c, TRAX_ERR_ARG, "too many triplets");
