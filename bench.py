@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-parity", action="store_true")
     p.add_argument("--no-align", action="store_true", help="skip the alignment (differentiable fit) measurement")
+    p.add_argument("--runtime-csv", default=None, help="write the timed steps as the reference's runtime csv")
     p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: autotuned)")
     p.add_argument("--no-tune", action="store_true", help="skip the autotuner (grid of the workload, default blocks)")
     p.add_argument("--tune-cache", default=None, help="JSON cache file of the autotuner")
@@ -277,6 +278,10 @@ def run_ours(args, ranks):
     kern = {k: [] for k in capi.Context.KERNELS}
     stage = {k: [] for k in capi.Context.STAGES}
     t_wall0 = time.perf_counter()
+    records = None
+    if args.runtime_csv:
+        from trax_gb300 import runtime_csv
+        records = runtime_csv.RuntimeRecords()
     for _ in range(args.steps):
         st = ctx.seed_batch(use_graph=True)
         dev_ms.append(st.device_ms)
@@ -285,7 +290,13 @@ def run_ours(args, ranks):
             kern[k].append(v)
         for k, v in s_ms.items():
             stage[k].append(v)
+        if records is not None:
+            records.add(batch.n_events, batch.n_layers, len(batch.lts), shape["predict_threads"], n_hits,
+                        int(batch.hit_id.astype(np.int64).max()), s_ms, k_ms)
     t_wall = time.perf_counter() - t_wall0
+    if records is not None:
+        with open(args.runtime_csv, "w") as f:
+            f.write(records.csv())
     clk = clocks.stop()
     ranks.barrier()
     my_time = sum(dev_ms) / 1e3

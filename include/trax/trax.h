@@ -162,7 +162,7 @@ int trax_prefix_sum(trax_ctx* ctx, uint32_t* data, uint64_t n);
  * no cudaMalloc, no cudaFree and no allocating library routine, and needs no
  * trax_ctx.
  *   - Its scratch (tile ticket, error word, one look-back status word per
- *     2048-element tile) is a fixed array inside the library, present on
+ *     4096-element tile) is a fixed array inside the library, present on
  *     every GPU that loads it until the process exits; n is therefore limited
  *     to TRAX_NOALLOC_SCAN_MAX elements, larger n returns TRAX_ERR_ARG.
  *   - The first call on a device looks up the array's device address
@@ -288,6 +288,79 @@ int trax_apply_alignment(trax_ctx* ctx, const double* align);
 /* Row -> triplet index (into trax_get_triplets' arrays) [n_fit], and the
  * sigma_tip used per layer triplet [n_lt]. */
 int trax_fit_get_rows(trax_ctx* ctx, uint32_t* triplet_index, float* sigma_tip);
+
+/* ------------------------------------------------------------ event files
+ * PEventContainer files (the reference's src/datastructures/serialize/
+ * Event.proto: PEvent { runNumber, lumiSection, eventNumber, repeated PHit
+ * { position, detectorType, layer, detectorId, hitId, simTrackID,
+ * simTrackPt } }) read with a wire-format decoder of our own.  Host-only: no
+ * context and no GPU. */
+typedef struct trax_event_set trax_event_set;
+int trax_events_read(const char* path, trax_event_set** events, uint64_t* n_events);
+void trax_events_free(trax_event_set* events);
+/* The hits of event e as stored; every output may be NULL (first call for
+ * n_hits).  xyz [3 n_hits]; run_lumi_event [3]. */
+int trax_events_raw(const trax_event_set* events, uint64_t e, uint64_t* n_hits, float* xyz, uint64_t* layer,
+                    uint64_t* det_id, uint64_t* hit_id, uint64_t* sim_track_id, float* sim_pt, int32_t* det_type,
+                    uint64_t* run_lumi_event);
+
+typedef struct trax_loaded_sizes {
+  uint64_t n_hits, n_events, n_layers, n_findable;
+} trax_loaded_sizes;
+/* HitCollection::addEvent (HitCollection.cpp:21-180) for events
+ * [first, first + count): hits of simulated tracks with pT >= min_pt; a track
+ * is findable when it has a hit on every layer of the layer triplets
+ * (num_tracks >= 0 stops after that many findable tracks; only_tracks drops
+ * the hits of the other tracks); per event the hits are bucketed by layer 1
+ * .. highest layer, findable tracks' hits after the others.  The hit_id
+ * column carries the simulated track id, as in the reference.  Call with
+ * NULL arrays first to get the sizes, then with arrays of those sizes:
+ * x, y, z, layer, det_id, hit_id, event [n_hits]; event_offsets [n_events];
+ * layer_hits, layer_offsets [n_events * n_layers] (offsets from the event's
+ * first hit); findable_id, findable_event [n_findable]. */
+int trax_events_load(const trax_event_set* events, uint64_t first, uint64_t count, const trax_layer_triplet* lt,
+                     int n_lt, float min_pt, int num_tracks, int only_tracks, trax_loaded_sizes* sizes, float* x,
+                     float* y, float* z, uint32_t* layer, uint32_t* det_id, uint32_t* hit_id, uint32_t* event,
+                     uint32_t* event_offsets, uint32_t* layer_hits, uint32_t* layer_offsets, uint32_t* findable_id,
+                     uint32_t* findable_event);
+
+/* GeometrySupplement from the reference's detector tables
+ * (TripletBuilder.cpp:140-184): radius_dictionary rows "entry,radius",
+ * detector_radius rows "detId,entry,layer"; min/max radius of layers
+ * 1..n_layers over their modules, (10000, 0) for a layer without any. */
+int trax_geometry_from_files(const char* radius_dictionary, const char* detector_radius, uint32_t n_layers,
+                             float* min_r, float* max_r);
+
+/* ------------------------------------------------------------ physics
+ * PhysicsRecord::fillData / merge / csvDump (PhysicsRecord.cpp:86-404):
+ * per event and layer triplet, the fraction of findable tracks with a
+ * triplet (efficiency), and the fractions of the segment's triplets that
+ * are fakes (hits of different tracks) or clones (a track's second and
+ * later triplets); merged over events into means and standard deviations
+ * per layer triplet, out[p] for p < n_lt, and over all of them in
+ * out[n_lt] (layer_triplet = n_lt + 1, as the reference's csv).  Host-only.
+ * hit_track_id: the track id of every hit the triplets index. */
+typedef struct trax_physics_record {
+  uint32_t layer_triplet;
+  uint64_t n;
+  double efficiency, efficiency_dev, fake_rate, fake_rate_dev, clone_rate, clone_rate_dev;
+} trax_physics_record;
+int trax_physics_triplets(const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, const uint32_t* offsets,
+                          uint32_t n_events, uint32_t n_lt, const uint32_t* hit_track_id, const uint32_t* findable_id,
+                          const uint32_t* findable_event, uint64_t n_findable, trax_physics_record* out);
+
+/* Track evaluation of TripletBuilder.cpp:840-1066: tracks of three or more
+ * triplets from the CA output (trax_get_tracks), clone removal (tracks that
+ * share at least 19 % of the shorter one's hits), real tracks (all hits of
+ * one simulated track), fake and clone rates over the filtered tracks and
+ * efficiency = distinct real tracks / total_tracks.  Host-only. */
+typedef struct trax_track_metrics {
+  uint64_t total, filtered, valid, valid_unique, fakes;
+  double fake_rate, clone_rate, efficiency;
+} trax_track_metrics;
+int trax_physics_tracks(const uint32_t* tracks, const uint32_t* track_offsets, uint64_t n_triplets,
+                        const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, const uint32_t* hit_track_id,
+                        uint64_t total_tracks, trax_track_metrics* out);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,292 @@
+"""Event files, the reference's event loader and the physics bookkeeping
+(host-only C ABI, no GPU): a PEventContainer written here by an independent
+protobuf encoder is read back field by field; the loader is compared with a
+plain-Python restatement of HitCollection::addEvent (HitCollection.cpp:21-180);
+the physics records with hand-counted cases; and, where the reference's
+ttbar fixture is present (this container only), its 10 events run through
+the oracle chain against the reference's published physics numbers, loosely."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from trax_gb300 import events
+
+REF = "/root/reference"
+TTBAR = os.path.join(REF, "plotting/data/physics/hits.ttBar.pb")
+
+
+# ---------------------------------------------------------------- encoder
+def _varint(v):
+    if v < 0:
+        v += 1 << 64
+    out = bytearray()
+    while True:
+        b = v & 0x7F
+        v >>= 7
+        if v:
+            out.append(b | 0x80)
+        else:
+            out.append(b)
+            return bytes(out)
+
+
+def _key(field, wt):
+    return _varint((field << 3) | wt)
+
+
+def _ld(field, payload):
+    return _key(field, 2) + _varint(len(payload)) + payload
+
+
+def _f32(field, v):
+    return _key(field, 5) + struct.pack("<f", v)
+
+
+def _vi(field, v):
+    return _key(field, 0) + _varint(v)
+
+
+def encode(events_):
+    out = b""
+    for ev in events_:
+        body = _vi(1, ev["run"]) + _vi(2, ev["lumi"]) + _vi(3, ev["event"])
+        for h in ev["hits"]:
+            pos = _f32(1, h["x"]) + _f32(2, h["y"]) + _f32(3, h["z"])
+            hb = _ld(1, pos) + _vi(2, h["type"]) + _vi(3, h["layer"]) + _vi(4, h["det"]) + _vi(5, h["hid"])
+            if h.get("sim") is not None:
+                hb += _vi(6, h["sim"])
+            if h.get("pt") is not None:
+                hb += _f32(7, h["pt"])
+            hb += _vi(15, 99)  # an unknown field, skipped by readers
+            body += _ld(4, hb)
+        out += _ld(1, body)
+    return out
+
+
+def synthetic_events(seed=3, n_events=4):
+    rng = np.random.default_rng(seed)
+    evs = []
+    for e in range(n_events):
+        hits = []
+        for t in range(1, 30):
+            pt = float(rng.uniform(0.3, 5.0))
+            layers = [l for l in range(1, 10) if rng.uniform() < 0.9]
+            for l in layers:
+                for _ in range(2 if rng.uniform() < 0.05 else 1):
+                    hits.append(dict(x=float(rng.normal()), y=float(rng.normal()), z=float(rng.normal()),
+                                     type=int(rng.integers(-1, 2)), layer=l, det=int(rng.integers(1, 1 << 33)),
+                                     hid=int(rng.integers(0, 1000)), sim=t, pt=pt))
+        for _ in range(20):  # unassociated hits: no simulated track, no pT
+            hits.append(dict(x=1.0, y=2.0, z=3.0, type=0, layer=int(rng.integers(1, 10)), det=5, hid=7,
+                             sim=None, pt=None))
+        order = rng.permutation(len(hits))
+        evs.append(dict(run=1, lumi=2, event=100 + e, hits=[hits[i] for i in order]))
+    return evs
+
+
+@pytest.fixture(scope="module")
+def eventio():
+    from trax_gb300 import build, eventio
+    build.build()
+    return eventio
+
+
+def test_reader_returns_every_field(eventio, tmp_path):
+    evs = synthetic_events()
+    p = tmp_path / "events.pb"
+    p.write_bytes(encode(evs))
+    f = eventio.EventFile(str(p))
+    assert f.n_events == len(evs)
+    for e, ev in enumerate(evs):
+        r = f.raw(e)
+        assert list(r["run_lumi_event"]) == [1, 2, 100 + e]
+        assert r["layer"].size == len(ev["hits"])
+        for i, h in enumerate(ev["hits"]):
+            assert tuple(r["xyz"][i]) == tuple(np.float32([h["x"], h["y"], h["z"]]))
+            assert r["det_type"][i] == h["type"] and r["layer"][i] == h["layer"] and r["det_id"][i] == h["det"]
+            assert r["hit_id"][i] == h["hid"]
+            assert r["sim_track_id"][i] == (h["sim"] or 0)
+            assert r["sim_pt"][i] == np.float32(h["pt"] or 0.0)
+
+
+def test_reader_rejects_truncated_files(eventio, tmp_path):
+    data = encode(synthetic_events(n_events=1))
+    p = tmp_path / "bad.pb"
+    p.write_bytes(data[:-7])
+    from trax_gb300 import capi
+    with pytest.raises(capi.TraxError):
+        eventio.EventFile(str(p))
+
+
+# ---------------------------------------------------------------- loader
+def add_event_restated(ev_hits, lts, min_pt, num_tracks=-1, only_tracks=False):
+    """HitCollection::addEvent in plain Python (test oracle)."""
+    used = sorted({l for t in lts for l in (t.layer1, t.layer2, t.layer3)})
+    max_layer = max(t.layer3 for t in lts)
+    tracks = {}
+    for h in ev_hits:
+        sim = h["sim_track_id"]
+        if only_tracks and sim == 0:
+            continue
+        if h["sim_pt"] < min_pt:
+            continue
+        tracks.setdefault(sim, []).append(h)
+    for k in tracks:
+        tracks[k] = sorted(tracks[k], key=lambda h: h["layer"])  # stable
+    layers, findable, found = {}, {}, 0
+    for tid in sorted(tracks):
+        if found == num_tracks:
+            break
+        if only_tracks and tid == 0:
+            continue
+        cov = {h["layer"] for h in tracks[tid] if 1 <= h["layer"] <= max_layer}
+        missing = any(l not in cov for l in used)
+        if tracks[tid][0]["sim_pt"] < min_pt:
+            continue
+        for h in tracks[tid]:
+            if not missing:
+                findable.setdefault(tid, []).append(h)
+            elif not only_tracks:
+                layers.setdefault(h["layer"], []).append(h)
+        if not missing:
+            found += 1
+    for tid in sorted(findable):
+        for h in findable[tid]:
+            if h["layer"] <= max_layer:
+                layers.setdefault(h["layer"], []).append(h)
+    hits = [h for l in range(1, max_layer + 1) for h in layers.get(l, [])]
+    counts = [len(layers.get(l, [])) for l in range(1, max_layer + 1)]
+    return hits, counts, sorted(findable)
+
+
+def _raw_hits(f, e):
+    r = f.raw(e)
+    return [dict(x=r["xyz"][i, 0], y=r["xyz"][i, 1], z=r["xyz"][i, 2], layer=int(r["layer"][i]),
+                 det=int(r["det_id"][i]), sim_track_id=int(r["sim_track_id"][i]), sim_pt=float(r["sim_pt"][i]))
+            for i in range(r["layer"].size)]
+
+
+def _check_loader(f, lts, min_pt, num_tracks, only_tracks):
+    batch, fid, fev = f.load(lts, min_pt, num_tracks=num_tracks, only_tracks=only_tracks)
+    for e in range(f.n_events):
+        want, counts, want_f = add_event_restated(_raw_hits(f, e), lts, min_pt, num_tracks, only_tracks)
+        a = int(batch.event_offsets[e])
+        n = int(batch.layer_hits[e].sum())
+        assert list(batch.layer_hits[e]) == counts
+        assert n == len(want)
+        got_layer = batch.layer[a:a + n]
+        assert list(got_layer) == [h["layer"] for h in want]
+        assert np.array_equal(batch.x[a:a + n], np.float32([h["x"] for h in want]))
+        assert list(batch.hit_id[a:a + n]) == [h["sim_track_id"] for h in want]
+        assert list(fid[fev == e]) == want_f
+
+
+@pytest.mark.parametrize("num_tracks,only_tracks", [(-1, False), (-1, True), (5, False)])
+def test_loader_matches_restated_add_event(eventio, tmp_path, num_tracks, only_tracks):
+    p = tmp_path / "events.pb"
+    p.write_bytes(encode(synthetic_events()))
+    f = eventio.EventFile(str(p))
+    lts = events.layer_triplets([1, 2, 3])
+    _check_loader(f, lts, 1.0, num_tracks, only_tracks)
+
+
+def test_geometry_from_tables(eventio, tmp_path):
+    d = tmp_path / "dict.dat"
+    g = tmp_path / "det.dat"
+    d.write_text("0,4.5\n1,4.1\n2,7.2\n3,7.6\n")
+    g.write_text("100,0,1\n101,1,1\n200,2,2\n201,3,2\n202,9,2\n")
+    mn, mx = eventio.geometry_from_files(str(d), str(g), 4)
+    assert np.allclose(mn, [4.1, 7.2, 10000, 10000]) and np.allclose(mx, [4.5, 7.6, 0, 0])
+
+
+# ---------------------------------------------------------------- physics
+def test_triplet_physics_hand_counted():
+    from trax_gb300 import build, physics
+    build.build()
+    # hits 0..8: track ids
+    tid = np.array([1, 1, 1, 2, 2, 2, 3, 4, 5], np.uint32)
+    # event 0, one layer triplet: two triplets of track 1 (one clone), one of track 2, one fake
+    h1, h2, h3 = [0, 0, 3, 6], [1, 1, 4, 7], [2, 2, 5, 8]
+    offsets = [0, 4]
+    recs = physics.triplet_records(h1, h2, h3, offsets, 1, 1, tid, [1, 2, 9], [0, 0, 0])
+    r = recs[0]
+    assert r["efficiency"] == pytest.approx(2 / 3)
+    assert r["fake_rate"] == pytest.approx(1 / 4)
+    assert r["clone_rate"] == pytest.approx(1 / 4)
+    assert recs[1]["layer_triplet"] == 2 and recs[1]["n"] == 1
+
+
+def test_track_metrics_hand_counted():
+    from trax_gb300 import build, physics
+    build.build()
+    # 5 triplets; CA tracks: triplet 4 -> [4, 3, 2] (3 triplets, a track), triplet 1 -> [1, 0] (too short)
+    h1 = [0, 1, 2, 3, 4]
+    h2 = [1, 2, 3, 4, 5]
+    h3 = [2, 3, 4, 5, 6]
+    tid = np.array([7] * 7, np.uint32)
+    tracks = [1, 0, 4, 3, 2]
+    track_offsets = [0, 0, 2, 2, 2, 5]
+    m = physics.track_metrics(tracks, track_offsets, h1, h2, h3, tid, 2)
+    assert m["total"] == 1 and m["filtered"] == 1 and m["valid_unique"] == 1 and m["fakes"] == 0
+    assert m["efficiency"] == pytest.approx(0.5)
+
+
+@pytest.mark.skipif(not os.path.exists(TTBAR), reason="the reference's ttbar fixture is not on this machine")
+def test_reference_ttbar_fixture(eventio, oracle_lib):
+    from trax_gb300 import physics
+    f = eventio.EventFile(TTBAR)
+    assert f.n_events == 10
+    sizes = [f.raw(e)["layer"].size for e in range(10)]
+    assert 900 <= min(sizes) and max(sizes) <= 2200
+    lts = events.layer_triplets([1, 2, 3, 4])
+    t = lts[3]
+    lts[3] = events.LayerTriplet(4, 5, 8, t.dtheta_cut, t.sigma_z, t.dphi_cut, t.sigma_phi, t.tip_cut,
+                                 t.pair_spread_z, t.z0, t.pair_spread_phi, t.n_candidates)
+    _check_loader(f, lts, 1.0, -1, True)
+    mn, mx = eventio.geometry_from_files(os.path.join(REF, "configs/radiusDictionary.dat"),
+                                         os.path.join(REF, "configs/detectorRadius.dat"), 13)
+    batch, fid, fev = f.load(lts, 1.0, only_tracks=True, n_z=50, n_phi=8, min_r=mn[:8], max_r=mx[:8])
+    r = oracle_lib.run(batch)[0]
+    hid = batch.hit_id[r["perm"]]
+    recs = physics.triplet_records(r["trip_h1"], r["trip_h2"], r["trip_h3"], r["trip_offsets"], batch.n_events,
+                                   len(lts), hid, fid, fev)
+    # the reference's numbers (plotting/data/physics/physics.ttBar.csv:2-6) come from 2000 events of
+    # a larger sample; on these 10 events: first-layer-triplet efficiency near its 0.79, totals in range
+    assert 0.7 <= recs[0]["efficiency"] <= 0.9
+    assert 0.5 <= recs[-1]["efficiency"] <= 0.9
+    assert recs[-1]["fake_rate"] <= 0.6 and recs[-1]["clone_rate"] <= 0.2
+
+
+@pytest.mark.gpu
+def test_loaded_events_on_the_gpu_match_the_oracle(eventio, oracle_lib, tmp_path):
+    """Events read and bucketed by the loader run through the GPU chain bit-exactly."""
+    from trax_gb300 import capi, physics
+    p = tmp_path / "events.pb"
+    evs = synthetic_events(seed=11, n_events=6)
+    for ev in evs:  # give the loaded hits a geometry the seeding windows accept: radii per layer
+        for h in ev["hits"]:
+            r = 4.0 + 3.0 * h["layer"]
+            n = np.hypot(h["x"], h["y"]) or 1.0
+            h["x"], h["y"], h["z"] = h["x"] / n * r, h["y"] / n * r, h["z"] * 5.0
+    p.write_bytes(encode(evs))
+    f = eventio.EventFile(str(p))
+    lts = events.layer_triplets([1, 2])
+    batch, fid, fev = f.load(lts, 1.0, n_z=20, n_phi=32)
+    ref = oracle_lib.run(batch)[0]
+    ctx = capi.Context(0)
+    try:
+        ctx.upload(batch)
+        ctx.seed_batch(use_graph=True)
+        got = ctx.results()
+    finally:
+        ctx.close()
+    for k in ("perm", "pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "trip_offsets"):
+        assert np.array_equal(np.asarray(got[k]), np.asarray(ref[k])), k
+    hid = batch.hit_id[got["perm"]]
+    a = physics.triplet_records(got["trip_h1"], got["trip_h2"], got["trip_h3"], got["trip_offsets"],
+                                batch.n_events, len(lts), hid, fid, fev)
+    b = physics.triplet_records(ref["trip_h1"], ref["trip_h2"], ref["trip_h3"], ref["trip_offsets"],
+                                batch.n_events, len(lts), hid, fid, fev)
+    assert a == b

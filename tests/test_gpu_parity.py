@@ -110,7 +110,7 @@ def test_single_event_single_track(ctx, oracle_lib):
     compare(got, ref)
 
 
-@pytest.mark.parametrize("n", [1, 2, 7, 2047, 2048, 2049, 123457, 4 * 1024 * 1024 + 3])
+@pytest.mark.parametrize("n", [1, 2, 7, 2047, 2048, 2049, 4095, 4096, 4097, 123457, 4 * 1024 * 1024 + 3])
 def test_prefix_sum_random(ctx, n):
     rng = np.random.default_rng(n)
     x = rng.integers(0, 1000, n, dtype=np.uint32)

@@ -21,7 +21,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/trax/trax.h"
+#include "trax/trax.h"
 #include "trax_kernels.h"
 
 using namespace trax;

@@ -17,7 +17,7 @@ namespace trax {
 namespace {
 
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_ITEMS = 16;
 constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __global__ void __launch_bounds__(SCAN_THREADS)
@@ -38,9 +38,14 @@ __global__ void __launch_bounds__(SCAN_THREADS)
   const uint64_t i0 = base + (uint64_t)threadIdx.x * SCAN_ITEMS;
   if (i0 + SCAN_ITEMS <= n && ((reinterpret_cast<uintptr_t>(in) & 15u) == 0)) {
     const uint4* p = reinterpret_cast<const uint4*>(in + i0);
-    uint4 a = p[0], b = p[1];
-    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
+      const uint4 a = p[q];
+      v[4 * q] = a.x;
+      v[4 * q + 1] = a.y;
+      v[4 * q + 2] = a.z;
+      v[4 * q + 3] = a.w;
+    }
   } else {
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) v[k] = (i0 + k < n) ? in[i0 + k] : 0u;
@@ -91,8 +96,9 @@ __global__ void __launch_bounds__(SCAN_THREADS)
   const uint32_t off = s_prefix + s_warp[warp] + (incl - sum);
   if (i0 + SCAN_ITEMS <= n && ((reinterpret_cast<uintptr_t>(out) & 15u) == 0)) {
     uint4* p = reinterpret_cast<uint4*>(out + i0);
-    p[0] = make_uint4(off + v[0], off + v[1], off + v[2], off + v[3]);
-    p[1] = make_uint4(off + v[4], off + v[5], off + v[6], off + v[7]);
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS / 4; ++q)
+      p[q] = make_uint4(off + v[4 * q], off + v[4 * q + 1], off + v[4 * q + 2], off + v[4 * q + 3]);
   } else {
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k)
@@ -205,7 +211,7 @@ cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint
 #include <cstdio>
 #include <mutex>
 
-#include "../../include/trax/trax.h"
+#include "trax/trax.h"
 
 namespace {
 
