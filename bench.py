@@ -167,6 +167,21 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells):
     }.get(name, 0)
 
 
+# DRAM bytes per unit of work of the kernels that can dominate the chain,
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
+# same chain on the first 300 events of the workload; a full launch scales
+# them by its units (traffic grows with pairs, candidates and hits).
+TRAFFIC_PER_UNIT = {"predict_count": ("pairs", 32.4), "filter": ("candidates", 28.5), "grid_build": ("hits", 124.2)}
+
+
+def kernel_traffic(name, st, n_hits):
+    if name not in TRAFFIC_PER_UNIT:
+        return None
+    unit, per = TRAFFIC_PER_UNIT[name]
+    n = {"pairs": st.n_pairs, "candidates": st.n_candidates, "hits": n_hits}[unit]
+    return int(per * n)
+
+
 def chain_bytes(st, n_hits, cells, n_layers):
     # per-batch algorithmic bytes of the whole chain: hits read and written by
     # the grid build, every intermediate array written once and read once,
@@ -338,7 +353,8 @@ def run_ours(args, ranks):
         "stage_ms": {k: round(float(np.mean(v)), 4) for k, v in stage.items() if v and min(v) >= 0},
         "kernel_ms": {k: round(v, 4) for k, v in kmean.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None,
+                     "frac": round(achieved / hbm, 4), "traffic": kernel_traffic(dom, st, n_hits),
+                     "traffic_note": "DRAM bytes per launch: ncu per-unit traffic of the 300-event case x units",
                      "peak_kind": f"{peak_kind} hbm_gbs (copy bandwidth)",
                      "algorithmic_bytes": int(kb)},
         "chain_roofline": {"achieved": round(cb / (ms_per_step * 1e-3) / 1e9, 2), "unit": "GB/s",
