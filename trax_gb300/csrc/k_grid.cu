@@ -74,36 +74,42 @@ __global__ void __launch_bounds__(GRID_THREADS)
   for (uint32_t w = 0; w < warp; ++w) warpOff += s_warpSum[w];
   uint32_t run = warpOff + incl - local;
   __syncthreads();
-  uint32_t* gl = grid + (size_t)task * C;
   for (uint32_t c = c0; c < c1; ++c) {
     uint32_t v = cnt[c];
     cnt[c] = run;  // becomes the next free slot of the cell
-    gl[c] = base + run;
     run += v;
   }
   __syncthreads();
+  // the boundaries, written with consecutive threads on consecutive cells
+  uint32_t* gl = grid + (size_t)task * C;
+  for (uint32_t c = tid; c < C; c += GRID_THREADS) gl[c] = base + cnt[c];
+  __syncthreads();
 
-  // 3. stable placement: chunks of GRID_THREADS hits in input order, warps
-  //    of a chunk take their turn so that lower input indices get lower slots
-  for (uint32_t c0h = 0; c0h < n; c0h += GRID_THREADS) {
-    const uint32_t i = c0h + tid;
-    const bool valid = i < n;
-    const uint32_t cell = valid ? sc.cell[base + i] : 0xffffffffu;
-    for (uint32_t w = 0; w < GRID_WARPS; ++w) {
-      if (warp == w && c0h + w * 32 < n) {
-        const uint32_t peers = __match_any_sync(0xffffffffu, cell);
-        if (valid) {
-          const uint32_t leader = __ffs(peers) - 1;
-          const uint32_t rank = __popc(peers & lanemask_lt());
-          uint32_t slot0 = 0;
-          if (lane == leader) slot0 = atomicAdd(&cnt[cell], (uint32_t)__popc(peers));
-          slot0 = __shfl_sync(peers, slot0, leader);
-          sc.perm[base + slot0 + rank] = i;
-        }
+  // 3. placement: a slot per hit from the cell cursors (shared-memory
+  //    atomics, any order inside a cell), then every cell's slots sorted by
+  //    input index -- the stable order, one of the orders the reference's
+  //    atomic_inc can produce.  After the atomics cnt[c] is the end of cell c,
+  //    and so the start of cell c + 1.
+  for (uint32_t i = tid; i < n; i += GRID_THREADS) {
+    const uint32_t cell = sc.cell[base + i];
+    sc.perm[base + atomicAdd(&cnt[cell], 1u)] = i;
+  }
+  __syncthreads();
+  for (uint32_t c = tid; c < C; c += GRID_THREADS) {
+    const uint32_t lo = c ? cnt[c - 1] : 0u, hi = cnt[c];
+    if (hi - lo < 2) continue;
+    uint32_t* p = sc.perm + base;
+    for (uint32_t a = lo + 1; a < hi; ++a) {  // insertion sort: cells hold a few hits
+      const uint32_t v = p[a];
+      uint32_t b = a;
+      while (b > lo && p[b - 1] > v) {
+        p[b] = p[b - 1];
+        --b;
       }
-      __syncthreads();
+      p[b] = v;
     }
   }
+  __syncthreads();
 
   // 4. gather into cell order (gridStore, GridBuilder.h:243-253)
   for (uint32_t s = tid; s < n; s += GRID_THREADS) {
