@@ -94,6 +94,14 @@ void trax_destroy(trax_ctx* ctx);
 const char* trax_last_error(const trax_ctx* ctx);
 const char* trax_version(void);
 
+/* Page-locked host memory for the arrays passed to trax_upload_hits and the
+ * trax_get_* calls: copies from and to it run at the link's DMA rate, copies
+ * from ordinary (pageable) memory go through a staging copy.  No counterpart
+ * in the reference (clever's buffers are OpenCL host-visible allocations).
+ * NULL on failure. */
+void* trax_host_alloc(size_t bytes);
+void trax_host_free(void* ptr);
+
 /* ---------------------------------------------------------- configuration
  * TripletConfigurations + minRadiusCurvature (TripletConfiguration.h:39-72,
  * TripletConfiguration.cpp:36-43).  Row p must have layer1 == p + 1 (the

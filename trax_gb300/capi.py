@@ -11,6 +11,7 @@ import ctypes
 import dataclasses
 import os
 import threading
+import weakref
 from typing import Dict, Optional
 
 import numpy as np
@@ -31,7 +32,8 @@ EXPORTED = [
     "trax_get_tracks", "trax_get_grid", "trax_get_hit_perm", "trax_set_block_sizes", "trax_get_launch_config",
     "trax_autotune", "trax_fit_prepare", "trax_fit_forward", "trax_fit_backward", "trax_fit_get_rows",
     "trax_apply_alignment", "trax_events_read", "trax_events_free", "trax_events_raw", "trax_events_load",
-    "trax_physics_triplets", "trax_physics_tracks", "trax_geometry_from_files",
+    "trax_physics_triplets", "trax_physics_tracks", "trax_geometry_from_files", "trax_host_alloc",
+    "trax_host_free",
 ]
 
 
@@ -144,6 +146,8 @@ def load() -> ctypes.CDLL:
             "trax_physics_triplets": ([vp, vp, vp, vp, u32, u32, vp, vp, vp, u64, vp], i32),
             "trax_physics_tracks": ([vp, vp, u64, vp, vp, vp, vp, u64, vp], i32),
             "trax_geometry_from_files": ([ctypes.c_char_p, ctypes.c_char_p, u32, vp, vp], i32),
+            "trax_host_alloc": ([ctypes.c_size_t], vp),
+            "trax_host_free": ([vp], None),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -151,6 +155,20 @@ def load() -> ctypes.CDLL:
             f.restype = res
         _lib = L
         return L
+
+
+def pinned_empty(shape, dtype) -> np.ndarray:
+    """A numpy array in page-locked host memory (trax_host_alloc), freed with the array."""
+    L = load()
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    ptr = L.trax_host_alloc(max(n, 1))
+    if not ptr:
+        raise MemoryError(f"trax_host_alloc({n}) failed")
+    buf = (ctypes.c_char * max(n, 1)).from_address(ptr)
+    arr = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+    weakref.finalize(buf, L.trax_host_free, ptr)
+    return arr
 
 
 def _p(a: Optional[np.ndarray]):
@@ -393,11 +411,15 @@ class Context:
         self._check(self._L.trax_get_candidates(self._h, _p(c), _p(o)))
         return c[:s.n_candidates], o
 
-    def triplets(self):
+    def triplets(self, out=None):
+        """(h1, h2, h3, offsets); `out` = four caller arrays large enough (e.g. pinned) to fill instead."""
         s = self.stats()
         n = max(s.n_triplets, 1)
-        h1, h2, h3 = (np.zeros(n, dtype=np.uint32) for _ in range(3))
-        o = np.zeros(self._n_offsets(), dtype=np.uint32)
+        if out is not None:
+            h1, h2, h3, o = out
+        else:
+            h1, h2, h3 = (np.zeros(n, dtype=np.uint32) for _ in range(3))
+            o = np.zeros(self._n_offsets(), dtype=np.uint32)
         self._check(self._L.trax_get_triplets(self._h, _p(h1), _p(h2), _p(h3), _p(o)))
         k = s.n_triplets
         return h1[:k], h2[:k], h3[:k], o
@@ -418,11 +440,15 @@ class Context:
         self._check(self._L.trax_get_links(self._h, _p(b), _p(f), _p(c), _p(nc)))
         return b[:s.n_links], f[:s.n_links], c[:s.n_connectable], nc[:s.n_non_connectable]
 
-    def tracks(self):
+    def tracks(self, out=None):
+        """(states, tracks, track offsets); `out` = three caller arrays large enough to fill instead."""
         s = self.stats()
-        states = np.zeros(max(s.n_triplets, 1), dtype=np.uint32)
-        tr = np.zeros(max(s.n_track_entries, 1), dtype=np.uint32)
-        off = np.zeros(s.n_triplets + 1, dtype=np.uint32)
+        if out is not None:
+            states, tr, off = out
+        else:
+            states = np.zeros(max(s.n_triplets, 1), dtype=np.uint32)
+            tr = np.zeros(max(s.n_track_entries, 1), dtype=np.uint32)
+            off = np.zeros(s.n_triplets + 1, dtype=np.uint32)
         self._check(self._L.trax_get_tracks(self._h, _p(states), _p(tr), _p(off)))
         if s.n_links == 0:
             return states[:0], tr[:0], off[:0]

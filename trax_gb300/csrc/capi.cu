@@ -944,6 +944,16 @@ int trax_set_grid(trax_ctx* c, uint32_t n_z, uint32_t n_phi) {
   return TRAX_OK;
 }
 
+void* trax_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  return p;
+}
+
+void trax_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
 int trax_set_block_sizes(trax_ctx* c, uint32_t pair_threads, uint32_t predict_threads, uint32_t filter_threads) {
   if (!c) return TRAX_ERR_ARG;
   for (uint32_t t : {pair_threads, predict_threads, filter_threads})
