@@ -145,23 +145,47 @@ __global__ void predict_offsets_kernel(uint32_t S, const uint32_t* __restrict__ 
     offsets[s] = s == 0 ? 0u : candStart[min(pairOffsets[s], nPairs)];
 }
 
-// filterCount (TripletThetaPhiFilter.h:65-154) for one candidate
-__device__ __forceinline__ bool filter_one(const DevConfig& cfg, const float4* hits, const uint32_t* hitLayer,
-                                           const uint2* pairs, uint2 cand) {
-  if (cand.y == TRAX_SENTINEL) return false;  // a slot the reference never wrote
-  const uint2 pr = pairs[cand.x];
-  const float4 A = hits[pr.x], B = hits[pr.y];
-  const FilterPair f = filter_prep(cfg, hitLayer[pr.x] - 1, A, B);
-  return filter_cand(cfg, f, B, hits[cand.y]);
-}
-
-__global__ void __launch_bounds__(256)
+// The flags in two steps per block of candidates: every candidate takes the
+// dphi test, which rejects most of them (two atan2); the block queues the
+// survivors and its threads then run the dtheta / TIP / curvature tests on
+// the queue, densely, instead of leaving rejected lanes idle beside them.
+// The flag is the AND of filterCount's four predicates (TripletThetaPhiFilter.h:65-154).
+__global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     filter_kernel(DevConfig cfg, const float4* __restrict__ hits, const uint32_t* __restrict__ hitLayer,
                   const uint2* __restrict__ pairs, const uint2* __restrict__ cands, const uint32_t* nCandsDev,
                   uint32_t* flags) {
+  __shared__ uint32_t s_queue[TRAX_MAX_TUNED_THREADS];
+  __shared__ uint32_t s_n;
   const uint32_t n = *nCandsDev;
-  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x)
-    flags[g] = filter_one(cfg, hits, hitLayer, pairs, cands[g]) ? 1u : 0u;
+  const uint32_t T = blockDim.x, lane = threadIdx.x & 31u;
+  for (uint32_t g0 = blockIdx.x * T; g0 < n; g0 += gridDim.x * T) {
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const uint32_t g = g0 + threadIdx.x;
+    bool pass = false;
+    if (g < n) {
+      const uint2 c = cands[g];
+      if (c.y != TRAX_SENTINEL) {  // a slot the reference never wrote fails
+        const uint2 pr = pairs[c.x];
+        pass = filter_dphi(cfg.dPhiCut[hitLayer[pr.x] - 1], hits[pr.x], hits[pr.y], hits[c.y]);
+      }
+      if (!pass) flags[g] = 0u;
+    }
+    const uint32_t ballot = __ballot_sync(0xffffffffu, pass);
+    uint32_t slot0 = 0;
+    if (lane == 0 && ballot) slot0 = atomicAdd(&s_n, (uint32_t)__popc(ballot));
+    slot0 = __shfl_sync(0xffffffffu, slot0, 0);
+    if (pass) s_queue[slot0 + __popc(ballot & lanemask_lt())] = g;
+    __syncthreads();
+    const uint32_t m = s_n;
+    for (uint32_t q = threadIdx.x; q < m; q += T) {
+      const uint32_t gq = s_queue[q];
+      const uint2 c = cands[gq];
+      const uint2 pr = pairs[c.x];
+      flags[gq] = filter_rest(cfg, hitLayer[pr.x] - 1, hits[pr.x], hits[pr.y], hits[c.y]) ? 1u : 0u;
+    }
+    __syncthreads();
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) flags[n] = 0u;
 }
 

@@ -1,6 +1,6 @@
 // trax_stages.cuh -- per-pair prediction window and per-candidate filter
-// predicate, shared by the stage-by-stage kernels and the fused batch kernel
-// so that both evaluate exactly the same float operations.
+// predicates, shared by the kernels of the prediction and filter stages
+// so that every pass evaluates exactly the same float operations.
 #pragma once
 
 #include "trax_device.cuh"
@@ -121,50 +121,41 @@ __device__ __forceinline__ void pred_row_parts(const PredWindow& w, const uint32
   }
 }
 
-// Per-pair part of filterCount (TripletThetaPhiFilter.h:84-107): the angles
-// of the first segment and the paraboloid point of the first hit.
-struct FilterPair {
-  float theta1, phi1;
-  f3 pP1, pP2;
-  float dThetaCut, dPhiCut, tipCut;
-};
-
-__device__ __forceinline__ FilterPair filter_prep(const DevConfig& cfg, uint32_t lt, float4 A, float4 B) {
-  FilterPair f;
-  f.dThetaCut = cfg.dThetaCut[lt];
-  f.dPhiCut = cfg.dPhiCut[lt];
-  f.tipCut = cfg.tipCut[lt];
-  f.theta1 = atan2_(sqrt_((B.x - A.x) * (B.x - A.x) + (B.y - A.y) * (B.y - A.y)), (B.z - A.z));
-  f.phi1 = atan2_((B.y - A.y), (B.x - A.x));
-  f.pP1 = make_f3(A.x, A.y, A.x * A.x + A.y * A.y);
-  f.pP2 = make_f3(B.x, B.y, B.x * B.x + B.y * B.y);
-  return f;
+// filterCount (TripletThetaPhiFilter.h:84-154) is the AND of four predicates
+// that share no state, so they can be evaluated in any order.  The dphi
+// part (:118-128): the transverse angles of the two segments.
+__device__ __forceinline__ bool filter_dphi(float dPhiCut, float4 A, float4 B, float4 Cc) {
+  const float phi1 = atan2_((B.y - A.y), (B.x - A.x));
+  const float phi2 = atan2_((Cc.y - B.y), (Cc.x - B.x));
+  float delta = phi2 - phi1;
+  delta += (delta > TRAX_PI_F) ? -2 * TRAX_PI_F : (delta < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
+  return fabs_(delta) <= dPhiCut;
 }
 
-// filterCount for the third hit Cc of the pair (A, B) (:84-154)
-__device__ __forceinline__ bool filter_cand(const DevConfig& cfg, const FilterPair& f, float4 B, float4 Cc) {
+// The dtheta, TIP and curvature parts (:84-117, :130-154).
+__device__ __forceinline__ bool filter_rest(const DevConfig& cfg, uint32_t lt, float4 A, float4 B, float4 Cc) {
   bool valid = true;
+  const float theta1 = atan2_(sqrt_((B.x - A.x) * (B.x - A.x) + (B.y - A.y) * (B.y - A.y)), (B.z - A.z));
   const float angle2 = atan2_(sqrt_((Cc.x - B.x) * (Cc.x - B.x) + (Cc.y - B.y) * (Cc.y - B.y)), (Cc.z - B.z));
-  float delta = fabs_(div_(angle2, f.theta1));
-  valid = valid && (1 - f.dThetaCut <= delta && delta <= 1 + f.dThetaCut);
-  const float phi2 = atan2_((Cc.y - B.y), (Cc.x - B.x));
-  delta = phi2 - f.phi1;
-  delta += (delta > TRAX_PI_F) ? -2 * TRAX_PI_F : (delta < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
-  valid = valid && (fabs_(delta) <= f.dPhiCut);
+  const float delta = fabs_(div_(angle2, theta1));
+  valid = valid && (1 - cfg.dThetaCut[lt] <= delta && delta <= 1 + cfg.dThetaCut[lt]);
+  const f3 pP1 = make_f3(A.x, A.y, A.x * A.x + A.y * A.y);
+  const f3 pP2 = make_f3(B.x, B.y, B.x * B.x + B.y * B.y);
   const f3 pP3 = make_f3(Cc.x, Cc.y, Cc.x * Cc.x + Cc.y * Cc.y);
-  const f3 a = sub3(f.pP2, f.pP1);
-  const f3 b = sub3(pP3, f.pP1);
+  const f3 a = sub3(pP2, pP1);
+  const f3 b = sub3(pP3, pP1);
   const f3 n = normalize3(cross3(a, b));
   const float cOx = div_(-n.x, 2 * n.z);
   const float cOy = div_(-n.y, 2 * n.z);
-  const float cc = -(n.x * f.pP1.x + n.y * f.pP1.y + n.z * f.pP1.z);
+  const float cc = -(n.x * pP1.x + n.y * pP1.y + n.z * pP1.z);
   const float cR = sqrt_(div_(1 - n.z * n.z - 4 * cc * n.z, 4 * n.z * n.z));
   float vx = -cOx, vy = -cOy;
   normalize2(vx, vy);
   const float pCAx = cOx + cR * vx;
   const float pCAy = cOy + cR * vy;
   const float tip_squared = pCAx * pCAx + pCAy * pCAy;
-  valid = valid && (tip_squared <= (f.tipCut * f.tipCut));
+  const float tipCut = cfg.tipCut[lt];
+  valid = valid && (tip_squared <= (tipCut * tipCut));
   valid = valid && (cR >= cfg.minRcurv);
   return valid;
 }
