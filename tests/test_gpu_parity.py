@@ -205,3 +205,36 @@ def test_config0_golden_gpu(ctx):
     got = stagewise(ctx, b)
     for k in ("grid", "perm", "pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "trip_offsets"):
         assert np.array_equal(got[k], d["oracle_" + k]), k
+
+
+def test_pileup_stress_event_matches_oracle(ctx, oracle_lib):
+    """The high-occupancy workload's event shape (vertices of 1000 tracks plus
+    noise, 10 layers, 6 layer triplets, grid 80 x 256), cut to three vertices
+    so that the oracle finishes in seconds."""
+    import dataclasses
+    w = dataclasses.replace(events.workload(3), n_events=2, n_vertices=6)
+    batch = events.generate_workload(w)
+    ref = oracle_lib.run(batch)[0]
+    ctx.upload(batch)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
+def test_capacity_overflow_recalibrates(ctx, oracle_lib):
+    """A batch of the same shape but far denser hits overflows the capacities
+    calibrated on the first: the call recalibrates, recaptures and returns the
+    exact result (admission never truncates)."""
+    sparse = events.generate(1, n_events=20)
+    ctx.upload(sparse)
+    calibrated = ctx.seed_batch(use_graph=True)
+    dense = events.generate(1, n_events=20)
+    rng = np.random.default_rng(5)
+    r = np.hypot(dense.x, dense.y)
+    phi = rng.uniform(-0.3, 0.3, r.size)  # every hit into one narrow phi wedge
+    dense.x = (r * np.cos(phi)).astype(np.float32)
+    dense.y = (r * np.sin(phi)).astype(np.float32)
+    ref = oracle_lib.run(dense)[0]
+    ctx.upload(dense)
+    st = ctx.seed_batch(use_graph=True)
+    assert st.n_pairs > 2 * calibrated.n_pairs  # beyond the calibrated headroom
+    compare(ctx.results(), ref)

@@ -292,7 +292,11 @@ def _helix_hits(vx, vy, vz, pt, eta, phi0, q, radius, b_field):
 
 def generate(config: int, n_events: Optional[int] = None, seed: Optional[int] = None) -> EventBatch:
     """Generate the workload `config` (0-4), optionally only its first events."""
-    w = workload(config, n_events)
+    return generate_workload(workload(config, n_events), seed)
+
+
+def generate_workload(w: Workload, seed: Optional[int] = None) -> EventBatch:
+    """Generate the events of a workload description."""
     rng = np.random.Generator(np.random.PCG64(w.seed if seed is None else seed))
     L = len(w.radii)
     radii = np.array(w.radii)
