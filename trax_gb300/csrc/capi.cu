@@ -66,6 +66,7 @@ enum Slot {
   S_CONN,
   S_NONCONN,
   S_TRACKS,
+  S_PRED_WARPS,
   S_N
 };
 
@@ -113,7 +114,7 @@ struct trax_ctx {
   // pair stage
   DevBuf segOuter, taskBase, taskCount, pairs, pairOffsets;
   // prediction / filter
-  DevBuf candCount, predKeep, cands, candOffsets, flags, h1, h2, h3, tripOffsets;
+  DevBuf candCount, predWarps, predKeep, cands, candOffsets, flags, h1, h2, h3, tripOffsets;
   // connectivity / fit / CA
   DevBuf eta, segOf, segStart, linkCount, cflags, basis, follower, connS, nonConnS, connIdx, nonConnIdx, pt;
   DevBuf states, inStart, inCursor, inList, best, isBest, handlers, tracks;
@@ -436,17 +437,21 @@ int stage_predict(trax_ctx* c, Mode mode) {
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   const uint32_t* nPairsDev = slot(c, S_PAIRS);
   const uint64_t maxPairs = mode == SYNCED ? c->nPairs : c->capPairs;
+  const uint64_t maxWarps = (maxPairs + 31) / 32;
   ENSURE(candCount, maxPairs + 1, 4);
+  ENSURE(predWarps, maxWarps + 1, 4);
   ENSURE(predKeep, maxPairs * TRAX_PRED_KEEP, 4);
   ENSURE(candOffsets, S + 1, 4);
   uint32_t* candCount = ptr<uint32_t>(c->candCount);
+  uint32_t* warpSums = ptr<uint32_t>(c->predWarps);
   KBEG(TK_PRED_COUNT);
   CK(predict_pairs(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
-                   candCount, ptr<uint32_t>(c->predKeep), nullptr, 0, slot(c, S_CAND_SENT), dev_err(c), c->st,
-                   &c->launches));
+                   candCount, warpSums, slot(c, S_PRED_WARPS), ptr<uint32_t>(c->predKeep), nullptr, 0,
+                   slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
   KEND(TK_PRED_COUNT);
-  RC(scan_publish(c, mode, candCount, c->nPairs, mode == DEVICE ? nPairsDev : nullptr, maxPairs, S_CANDS,
-                  mode == DEVICE ? c->capCands : NO_CAP));
+  // the prefix sum runs over the per-warp sums of the counts
+  RC(scan_publish(c, mode, warpSums, (c->nPairs + 31) / 32, mode == DEVICE ? slot(c, S_PRED_WARPS) : nullptr,
+                  maxWarps, S_CANDS, mode == DEVICE ? c->capCands : NO_CAP));
   uint64_t maxCands = c->capCands;
   if (mode == SYNCED) {
     RC(read_slot(c, S_CANDS, &c->nCands));
@@ -455,11 +460,11 @@ int stage_predict(trax_ctx* c, Mode mode) {
   ENSURE(cands, maxCands, 8);
   KBEG(TK_PRED_EMIT);
   CK(predict_pairs(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
-                   candCount, ptr<uint32_t>(c->predKeep), ptr<uint2>(c->cands), maxCands, slot(c, S_CAND_SENT),
-                   dev_err(c), c->st, &c->launches));
+                   candCount, warpSums, nullptr, ptr<uint32_t>(c->predKeep), ptr<uint2>(c->cands), maxCands,
+                   slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
   KEND(TK_PRED_EMIT);
-  CK(predict_offsets(c->cfg, ptr<uint32_t>(c->pairOffsets), nPairsDev, candCount, ptr<uint32_t>(c->candOffsets), c->st,
-                     &c->launches));
+  CK(predict_offsets(c->cfg, ptr<uint32_t>(c->pairOffsets), nPairsDev, candCount, warpSums,
+                     ptr<uint32_t>(c->candOffsets), c->st, &c->launches));
   return TRAX_OK;
 }
 
@@ -689,6 +694,7 @@ int size_device_buffers(trax_ctx* c) {
   ENSURE(taskCount, c->capTasks + 1, 4);
   ENSURE(pairs, c->capPairs, 8);
   ENSURE(candCount, c->capPairs + 1, 4);
+  ENSURE(predWarps, (c->capPairs + 31) / 32 + 1, 4);
   ENSURE(predKeep, c->capPairs * TRAX_PRED_KEEP, 4);
   ENSURE(cands, c->capCands, 8);
   ENSURE(flags, c->capCands + 1, 4);
@@ -884,7 +890,7 @@ void trax_destroy(trax_ctx* c) {
   DevBuf* bufs[] = {&c->in_x, &c->in_y, &c->in_z, &c->in_layer, &c->in_det, &c->in_hid, &c->in_evt, &c->evOff,
                     &c->layHits, &c->layOff, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
-                    &c->segOuter, &c->taskBase, &c->taskCount, &c->pairs, &c->pairOffsets, &c->candCount, &c->predKeep, &c->cands,
+                    &c->segOuter, &c->taskBase, &c->taskCount, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flags, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,

@@ -32,14 +32,23 @@ int grid_for(uint64_t items, int threads) {
 // min(count, TRAX_PRED_KEEP) candidates the store pass would write (the store
 // variant's valid hits, capped at the count; slots it would leave unwritten
 // get the sentinel), so that the store pass is a copy for most pairs.
+// The prefix sum between predictCount and predictStore is split in two:
+// every warp scans its 32 consecutive counts with shuffles and writes the
+// exclusive offsets within the warp to candCount and the warp's sum to
+// warpSums; only those sums (one per 32 pairs) are then scanned, and a
+// pair's position is its warp's scanned sum plus its offset in the warp.
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     predict_count_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
                          const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev, uint32_t* candCount,
-                         uint32_t* keep) {
+                         uint32_t* keep, uint32_t* warpSums, uint32_t* nWarpsOut, uint32_t* err) {
   const uint32_t nPairs = *nPairsDev;
-  for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < nPairs; gid += gridDim.x * blockDim.x) {
-    const uint2 pr = pairs[gid];
+  const uint32_t lane = threadIdx.x & 31u;
+  // warp-uniform loop: each warp covers 32 consecutive pairs per step
+  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nPairs;
+       base += gridDim.x * blockDim.x) {
+    const uint32_t gid = base + lane;
+    const uint2 pr = gid < nPairs ? pairs[gid] : make_uint2(TRAX_SENTINEL, TRAX_SENTINEL);
     uint32_t count = 0;
     if (pr.x != TRAX_SENTINEL) {
       const uint32_t event = hitEvt[pr.x];
@@ -77,9 +86,26 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
       const uint32_t k = min(count, (uint32_t)TRAX_PRED_KEEP);
       for (uint32_t q = nStore; q < k; ++q) slot[q] = TRAX_SENTINEL;
     }
-    candCount[gid] = count;
+    uint32_t incl = count;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= (uint32_t)d) incl += t;
+    }
+    if (gid < nPairs) candCount[gid] = incl - count;
+    // 32 counts can pass 2^32 only if one of them reaches 2^27
+    if (__reduce_max_sync(0xffffffffu, count) >= (1u << 27)) {
+      unsigned long long sum = count;
+      for (int d = 16; d > 0; d >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, d);
+      if (lane == 0 && sum > 0xffffffffull) raise_error(err, TRAX_EBIT_OVERFLOW);
+    }
+    if (lane == 31) warpSums[base >> 5] = incl;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) candCount[nPairs] = 0u;  // the scan's +1 slot
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint32_t nW = (nPairs + 31u) >> 5;
+    warpSums[nW] = 0u;  // the scan's +1 slot
+    *nWarpsOut = nW;
+  }
 }
 
 // Store pass (predictStore, :358-402): candidates (pair, hit3) at the
@@ -89,13 +115,16 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     predict_store_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
                          const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev,
-                         const uint32_t* __restrict__ candStart, const uint32_t* __restrict__ keep, uint2* cands,
-                         uint32_t capCands, uint32_t* sentinels) {
+                         const uint32_t* __restrict__ local, const uint32_t* __restrict__ warpStart,
+                         const uint32_t* __restrict__ keep, uint2* cands, uint32_t capCands, uint32_t* sentinels) {
   const uint32_t nPairs = *nPairsDev;
   uint32_t sent = 0;
   for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < nPairs; gid += gridDim.x * blockDim.x) {
-    const uint32_t pos = candStart[gid];
-    uint32_t limit = candStart[gid + 1] - pos;
+    const uint32_t wi = gid >> 5;
+    const uint32_t off = local[gid];
+    const uint32_t pos = warpStart[wi] + off;
+    // the next pair's position: the next warp's start after a warp's last pair
+    uint32_t limit = ((gid & 31u) == 31u || gid + 1 == nPairs) ? warpStart[wi + 1] - pos : local[gid + 1] - off;
     if (pos >= capCands) limit = 0;
     else if (limit > capCands - pos) limit = capCands - pos;
     if (limit == 0) continue;
@@ -138,11 +167,17 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
 // candidates, so both come down to the candidate position at the segment's
 // pair end.
 __global__ void predict_offsets_kernel(uint32_t S, const uint32_t* __restrict__ pairOffsets,
-                                       const uint32_t* __restrict__ nPairsDev, const uint32_t* __restrict__ candStart,
-                                       uint32_t* offsets) {
+                                       const uint32_t* __restrict__ nPairsDev, const uint32_t* __restrict__ local,
+                                       const uint32_t* __restrict__ warpStart, uint32_t* offsets) {
   const uint32_t nPairs = *nPairsDev;
-  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= S; s += gridDim.x * blockDim.x)
-    offsets[s] = s == 0 ? 0u : candStart[min(pairOffsets[s], nPairs)];
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s <= S; s += gridDim.x * blockDim.x) {
+    if (s == 0) {
+      offsets[0] = 0u;
+      continue;
+    }
+    const uint32_t p = min(pairOffsets[s], nPairs);
+    offsets[s] = p == nPairs ? warpStart[(nPairs + 31u) >> 5] : warpStart[p >> 5] + local[p];
+  }
 }
 
 // The flags in two steps per block of candidates: every candidate takes the
@@ -228,29 +263,30 @@ __global__ void triplet_offsets_kernel(DevConfig cfg, const uint32_t* __restrict
 }  // namespace
 
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
-                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* keep,
-                          uint2* cands, uint64_t capCands, uint32_t* sentinels, uint32_t* err, cudaStream_t st,
-                          uint32_t* launches) {
-  (void)err;
+                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* warpSums,
+                          uint32_t* nWarpsOut, uint32_t* keep, uint2* cands, uint64_t capCands, uint32_t* sentinels,
+                          uint32_t* err, cudaStream_t st, uint32_t* launches) {
   const uint32_t cap = capCands > 0xffffffffull ? 0xffffffffu : (uint32_t)capCands;
   const int threads = (int)cfg.predThreads;
   const int blocks = grid_for(maxPairs + 1, threads);
   if (emit) {
     if (maxPairs == 0) return cudaSuccess;
     predict_store_kernel<<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                          nPairsDev, candCount, keep, cands, cap, sentinels);
+                                                          nPairsDev, candCount, warpSums, keep, cands, cap, sentinels);
   } else {
     predict_count_kernel<<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                          nPairsDev, candCount, keep);
+                                                          nPairsDev, candCount, keep, warpSums, nWarpsOut, err);
   }
   if (launches) *launches += 1;
   return cudaGetLastError();
 }
 
 cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, const uint32_t* nPairsDev,
-                            const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st, uint32_t* launches) {
+                            const uint32_t* candCount, const uint32_t* warpStart, uint32_t* candOffsets,
+                            cudaStream_t st, uint32_t* launches) {
   const uint32_t S = cfg.E * cfg.nLT;
-  predict_offsets_kernel<<<grid_for(S + 1, 256), 256, 0, st>>>(S, pairOffsets, nPairsDev, candStart, candOffsets);
+  predict_offsets_kernel<<<grid_for(S + 1, 256), 256, 0, st>>>(S, pairOffsets, nPairsDev, candCount, warpStart,
+                                                               candOffsets);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

@@ -65,20 +65,25 @@ cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const u
                          uint32_t* pairOffsets, cudaStream_t st, uint32_t* launches);
 
 // ------------------------------------------------------------ prediction
-// Count pass (emit == false): candCount[nPairs+1] (+1 slot zeroed) and up to
-// TRAX_PRED_KEEP captured candidates per pair in keep[nPairs * TRAX_PRED_KEEP];
-// store pass (emit == true): candidates at the scanned positions candCount[].
+// Count pass (emit == false): per pair the exclusive offset of its
+// candidates within its warp of 32 pairs (candCount[nPairs]), the sum of
+// each warp's counts in warpSums[ceil(nPairs/32) + 1] (+1 slot zeroed; the
+// number of sums goes to *nWarpsOut) and up to TRAX_PRED_KEEP captured
+// candidates per pair in keep[nPairs * TRAX_PRED_KEEP]; store pass
+// (emit == true): with warpSums exclusively scanned, candidates at
+// warpSums[gid / 32] + candCount[gid].
 #define TRAX_PRED_KEEP 4
 
 // grids of up to this many cells per layer are built with shared-memory
 // counters (4 bytes per cell)
 #define TRAX_GRID_SMEM_CELLS 53248u
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
-                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* keep,
-                          uint2* cands, uint64_t capCands, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
-                          uint32_t* launches);
+                          const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* warpSums,
+                          uint32_t* nWarpsOut, uint32_t* keep, uint2* cands, uint64_t capCands,
+                          uint32_t* sentinelCount, uint32_t* err, cudaStream_t st, uint32_t* launches);
 cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, const uint32_t* nPairsDev,
-                            const uint32_t* candStart, uint32_t* candOffsets, cudaStream_t st, uint32_t* launches);
+                            const uint32_t* candCount, const uint32_t* warpStart, uint32_t* candOffsets,
+                            cudaStream_t st, uint32_t* launches);
 
 // ---------------------------------------------------------------- filter
 cudaError_t filter_candidates(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint2* cands,
