@@ -67,6 +67,7 @@ enum Slot {
   S_NONCONN,
   S_TRACKS,
   S_PRED_WARPS,
+  S_FLAG_WORDS,
   S_N
 };
 
@@ -114,7 +115,7 @@ struct trax_ctx {
   // pair stage
   DevBuf segOuter, taskBase, taskCount, pairs, pairOffsets;
   // prediction / filter
-  DevBuf candCount, predWarps, predKeep, cands, candOffsets, flags, h1, h2, h3, tripOffsets;
+  DevBuf candCount, predWarps, predKeep, cands, candOffsets, flagWords, flagSums, h1, h2, h3, tripOffsets;
   // connectivity / fit / CA
   DevBuf eta, segOf, segStart, linkCount, cflags, basis, follower, connS, nonConnS, connIdx, nonConnIdx, pt;
   DevBuf states, inStart, inCursor, inList, best, isBest, handlers, tracks;
@@ -472,15 +473,19 @@ int stage_filter(trax_ctx* c, Mode mode) {
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   const uint32_t* nCandsDev = slot(c, S_CANDS);
   const uint64_t maxCands = mode == SYNCED ? c->nCands : c->capCands;
-  ENSURE(flags, maxCands + 1, 4);
+  const uint64_t maxWords = (maxCands + 31) / 32;
+  ENSURE(flagWords, maxWords + 1, 4);
+  ENSURE(flagSums, maxWords + 1, 4);
   ENSURE(tripOffsets, S + 1, 4);
-  uint32_t* flags = ptr<uint32_t>(c->flags);
+  uint32_t* words = ptr<uint32_t>(c->flagWords);
+  uint32_t* sums = ptr<uint32_t>(c->flagSums);
   KBEG(TK_FILTER);
-  CK(filter_candidates(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, flags,
-                       c->st, &c->launches));
+  CK(filter_candidates(c->cfg, dev_hits(c), ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, words,
+                       sums, slot(c, S_FLAG_WORDS), c->st, &c->launches));
   KEND(TK_FILTER);
-  RC(scan_publish(c, mode, flags, c->nCands, mode == DEVICE ? nCandsDev : nullptr, maxCands, S_TRIPLETS,
-                  mode == DEVICE ? c->capT : NO_CAP));
+  // the prefix sum runs over the numbers of flags per word of 32 candidates
+  RC(scan_publish(c, mode, sums, (c->nCands + 31) / 32, mode == DEVICE ? slot(c, S_FLAG_WORDS) : nullptr, maxWords,
+                  S_TRIPLETS, mode == DEVICE ? c->capT : NO_CAP));
   uint64_t maxT = c->capT;
   if (mode == SYNCED) {
     RC(read_slot(c, S_TRIPLETS, &c->nT));
@@ -490,7 +495,7 @@ int stage_filter(trax_ctx* c, Mode mode) {
   ENSURE(h2, maxT, 4);
   ENSURE(h3, maxT, 4);
   KBEG(TK_FILTER_STORE);
-  CK(filter_store(ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, flags, ptr<uint32_t>(c->h1),
+  CK(filter_store(ptr<uint2>(c->pairs), ptr<uint2>(c->cands), nCandsDev, maxCands, words, sums, ptr<uint32_t>(c->h1),
                   ptr<uint32_t>(c->h2), ptr<uint32_t>(c->h3), maxT, c->st, &c->launches));
   KEND(TK_FILTER_STORE);
   CK(triplet_offsets(c->cfg, dev_hits(c), ptr<uint32_t>(c->h1), slot(c, S_TRIPLETS), maxT,
@@ -697,7 +702,8 @@ int size_device_buffers(trax_ctx* c) {
   ENSURE(predWarps, (c->capPairs + 31) / 32 + 1, 4);
   ENSURE(predKeep, c->capPairs * TRAX_PRED_KEEP, 4);
   ENSURE(cands, c->capCands, 8);
-  ENSURE(flags, c->capCands + 1, 4);
+  ENSURE(flagWords, (c->capCands + 31) / 32 + 1, 4);
+  ENSURE(flagSums, (c->capCands + 31) / 32 + 1, 4);
   ENSURE(h1, c->capT, 4); ENSURE(h2, c->capT, 4); ENSURE(h3, c->capT, 4);
   ENSURE(eta, c->capT, 4); ENSURE(segOf, c->capT, 4); ENSURE(segStart, S + 1, 4);
   ENSURE(linkCount, c->capT + 1, 4); ENSURE(cflags, c->capT + 1, 4);
@@ -891,7 +897,7 @@ void trax_destroy(trax_ctx* c) {
                     &c->layHits, &c->layOff, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
                     &c->segOuter, &c->taskBase, &c->taskCount, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
-                    &c->candOffsets, &c->flags, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
+                    &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,
                     &c->isBest, &c->handlers, &c->tracks, &c->scanScratch, &c->slots, &c->fitOk, &c->fitSegCnt,

@@ -10,8 +10,9 @@
 //
 // The filter replaces filterCount / filterPopCount / PrefixSum / filterStore /
 // filterOffsetStore / filterOffsetMonotonizeStore (TripletThetaPhiFilter.h:50-280,
-// .cpp:10-206): a flag per candidate, a scan of the flags and a stable
-// scatter of (h1, h2, h3) keep the candidate order of the reference.
+// .cpp:10-206): a flag per candidate (one bit of a word of 32), a scan of
+// the words' counts and a stable scatter of (h1, h2, h3) keep the candidate
+// order of the reference.
 #include "trax_kernels.h"
 #include "trax_stages.cuh"
 
@@ -185,16 +186,23 @@ __global__ void predict_offsets_kernel(uint32_t S, const uint32_t* __restrict__ 
 // survivors and its threads then run the dtheta / TIP / curvature tests on
 // the queue, densely, instead of leaving rejected lanes idle beside them.
 // The flag is the AND of filterCount's four predicates (TripletThetaPhiFilter.h:65-154).
+// filterPopCount + PrefixSum run on words of 32 flags: each warp of 32
+// consecutive candidates stores its flags as one ballot mask and their
+// number in warpSums (+1 slot zeroed, the number of words to *nWordsOut),
+// and only those sums are scanned; a triplet's position is its word's
+// scanned sum plus the flags set below it in the word.
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     filter_kernel(DevConfig cfg, const float4* __restrict__ hits, const uint32_t* __restrict__ hitLayer,
                   const uint2* __restrict__ pairs, const uint2* __restrict__ cands, const uint32_t* nCandsDev,
-                  uint32_t* flags) {
+                  uint32_t* masks, uint32_t* warpSums, uint32_t* nWordsOut) {
   __shared__ uint32_t s_queue[TRAX_MAX_TUNED_THREADS];
+  __shared__ uint8_t s_flag[TRAX_MAX_TUNED_THREADS];
   __shared__ uint32_t s_n;
   const uint32_t n = *nCandsDev;
   const uint32_t T = blockDim.x, lane = threadIdx.x & 31u;
   for (uint32_t g0 = blockIdx.x * T; g0 < n; g0 += gridDim.x * T) {
     if (threadIdx.x == 0) s_n = 0;
+    s_flag[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t g = g0 + threadIdx.x;
     bool pass = false;
@@ -204,33 +212,46 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
         const uint2 pr = pairs[c.x];
         pass = filter_dphi(cfg.dPhiCut[hitLayer[pr.x] - 1], hits[pr.x], hits[pr.y], hits[c.y]);
       }
-      if (!pass) flags[g] = 0u;
     }
     const uint32_t ballot = __ballot_sync(0xffffffffu, pass);
     uint32_t slot0 = 0;
     if (lane == 0 && ballot) slot0 = atomicAdd(&s_n, (uint32_t)__popc(ballot));
     slot0 = __shfl_sync(0xffffffffu, slot0, 0);
-    if (pass) s_queue[slot0 + __popc(ballot & lanemask_lt())] = g;
+    if (pass) s_queue[slot0 + __popc(ballot & lanemask_lt())] = threadIdx.x;
     __syncthreads();
     const uint32_t m = s_n;
     for (uint32_t q = threadIdx.x; q < m; q += T) {
-      const uint32_t gq = s_queue[q];
-      const uint2 c = cands[gq];
+      const uint32_t t = s_queue[q];
+      const uint2 c = cands[g0 + t];
       const uint2 pr = pairs[c.x];
-      flags[gq] = filter_rest(cfg, hitLayer[pr.x] - 1, hits[pr.x], hits[pr.y], hits[c.y]) ? 1u : 0u;
+      s_flag[t] = filter_rest(cfg, hitLayer[pr.x] - 1, hits[pr.x], hits[pr.y], hits[c.y]) ? 1 : 0;
+    }
+    __syncthreads();
+    const uint32_t word = __ballot_sync(0xffffffffu, s_flag[threadIdx.x] != 0);
+    if (lane == 0 && g < n) {
+      masks[g >> 5] = word;
+      warpSums[g >> 5] = (uint32_t)__popc(word);
     }
     __syncthreads();
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) flags[n] = 0u;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint32_t nW = (n + 31u) >> 5;
+    warpSums[nW] = 0u;  // the scan's +1 slot
+    *nWordsOut = nW;
+  }
 }
 
+// filterStore: (h1, h2, h3) of every flagged candidate, in candidate order
 __global__ void filter_store_kernel(const uint2* __restrict__ pairs, const uint2* __restrict__ cands,
-                                    const uint32_t* nCandsDev, const uint32_t* __restrict__ scan, uint32_t* h1,
-                                    uint32_t* h2, uint32_t* h3, uint32_t capT) {
+                                    const uint32_t* nCandsDev, const uint32_t* __restrict__ masks,
+                                    const uint32_t* __restrict__ wordStart, uint32_t* h1, uint32_t* h2, uint32_t* h3,
+                                    uint32_t capT) {
   const uint32_t n = *nCandsDev;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < n; g += gridDim.x * blockDim.x) {
-    const uint32_t pos = scan[g];
-    if (scan[g + 1] != pos && pos < capT) {
+    const uint32_t word = masks[g >> 5], bit = g & 31u;
+    if (!((word >> bit) & 1u)) continue;
+    const uint32_t pos = wordStart[g >> 5] + (uint32_t)__popc(word & ((1u << bit) - 1u));
+    if (pos < capT) {
       const uint2 c = cands[g];
       const uint2 p = pairs[c.x];
       h1[pos] = p.x;
@@ -292,20 +313,22 @@ cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, c
 }
 
 cudaError_t filter_candidates(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint2* cands,
-                              const uint32_t* nCandsDev, uint64_t maxCands, uint32_t* flags, cudaStream_t st,
-                              uint32_t* launches) {
-  filter_kernel<<<grid_for(maxCands + 1, (int)cfg.filterThreads), (int)cfg.filterThreads, 0, st>>>(cfg, hits.xyzp, hits.layer, pairs, cands, nCandsDev,
-                                                              flags);
+                              const uint32_t* nCandsDev, uint64_t maxCands, uint32_t* masks, uint32_t* warpSums,
+                              uint32_t* nWordsOut, cudaStream_t st, uint32_t* launches) {
+  const int threads = (int)cfg.filterThreads;
+  filter_kernel<<<grid_for(maxCands + 1, threads), threads, 0, st>>>(cfg, hits.xyzp, hits.layer, pairs, cands,
+                                                                     nCandsDev, masks, warpSums, nWordsOut);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }
 
 cudaError_t filter_store(const uint2* pairs, const uint2* cands, const uint32_t* nCandsDev, uint64_t maxCands,
-                         const uint32_t* flagScan, uint32_t* h1, uint32_t* h2, uint32_t* h3, uint64_t capT,
-                         cudaStream_t st, uint32_t* launches) {
+                         const uint32_t* masks, const uint32_t* wordStart, uint32_t* h1, uint32_t* h2, uint32_t* h3,
+                         uint64_t capT, cudaStream_t st, uint32_t* launches) {
   if (maxCands == 0) return cudaSuccess;
   const uint32_t cap = capT > 0xffffffffull ? 0xffffffffu : (uint32_t)capT;
-  filter_store_kernel<<<grid_for(maxCands, 256), 256, 0, st>>>(pairs, cands, nCandsDev, flagScan, h1, h2, h3, cap);
+  filter_store_kernel<<<grid_for(maxCands, 256), 256, 0, st>>>(pairs, cands, nCandsDev, masks, wordStart, h1, h2,
+                                                               h3, cap);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

@@ -86,12 +86,17 @@ cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, c
                             cudaStream_t st, uint32_t* launches);
 
 // ---------------------------------------------------------------- filter
+// the flags of 32 consecutive candidates as one word masks[g / 32] (bit
+// g % 32), the number of flags set per word in warpSums[ceil(n/32) + 1]
+// (+1 slot zeroed; the number of words goes to *nWordsOut)
 cudaError_t filter_candidates(const DevConfig& cfg, DevHits hits, const uint2* pairs, const uint2* cands,
-                              const uint32_t* nCandsDev, uint64_t maxCands, uint32_t* flags, cudaStream_t st,
-                              uint32_t* launches);
+                              const uint32_t* nCandsDev, uint64_t maxCands, uint32_t* masks, uint32_t* warpSums,
+                              uint32_t* nWordsOut, cudaStream_t st, uint32_t* launches);
+// with warpSums exclusively scanned into wordStart: the triplets of the
+// flagged candidates at wordStart[g / 32] + (flags below g in its word)
 cudaError_t filter_store(const uint2* pairs, const uint2* cands, const uint32_t* nCandsDev, uint64_t maxCands,
-                         const uint32_t* flagScan, uint32_t* h1, uint32_t* h2, uint32_t* h3, uint64_t capT,
-                         cudaStream_t st, uint32_t* launches);
+                         const uint32_t* masks, const uint32_t* wordStart, uint32_t* h1, uint32_t* h2, uint32_t* h3,
+                         uint64_t capT, cudaStream_t st, uint32_t* launches);
 // trackletOffsets with the reference's filterOffsetStore + monotonize semantics
 cudaError_t triplet_offsets(const DevConfig& cfg, DevHits hits, const uint32_t* h1, const uint32_t* nTDev,
                             uint64_t maxT, uint32_t* offsets, cudaStream_t st, uint32_t* launches);
