@@ -77,6 +77,36 @@ def test_batched_graph_matches_oracle(ctx, oracle_lib, config, n_events):
     compare(ctx.results(), ref)
 
 
+def test_warp_tile_boundaries(ctx, oracle_lib):
+    """Pair and candidate counts are scanned per warp of 32 (offsets within
+    the warp plus a scan of the warp sums) and the filter flags are packed 32
+    to a word: many small batches put the counts on many residues mod 32,
+    including partial last words and single-pair batches."""
+    residues = {"pairs": set(), "cands": set()}
+    for seed in range(12):
+        n_events = 1 + seed % 4
+        batch = events.generate(0 if seed % 3 == 0 else 1, n_events=n_events, seed=100 + seed)
+        ref = oracle_lib.run(batch)[0]
+        compare(stagewise(ctx, batch), ref)
+        ctx.seed_batch(use_graph=True)
+        compare(ctx.results(), ref)
+        residues["pairs"].add(int(ref["pairs"].shape[0]) % 32)
+        residues["cands"].add(int(ref["cands"].shape[0]) % 32)
+    assert len(residues["pairs"]) >= 6 and len(residues["cands"]) >= 6, residues
+    # no pairs at all: only the first layer keeps its hits
+    batch = events.generate(1, n_events=3, seed=7)
+    keep = batch.layer == 1
+    lh = batch.layer_hits.copy()
+    lh[:, 1:] = 0
+    sub = events._assemble({k: getattr(batch, k)[keep] for k in ("x", "y", "z", "layer", "det_id", "hit_id", "event")},
+                           lh, batch)
+    ref = oracle_lib.run(sub)[0]
+    assert ref["pairs"].shape[0] == 0
+    compare(stagewise(ctx, sub), ref)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
 def test_batched_synced_matches_graph(ctx, oracle_lib):
     batch = events.generate(2, n_events=4)
     ctx.upload(batch)

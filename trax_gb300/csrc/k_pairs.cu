@@ -83,6 +83,26 @@ __device__ __forceinline__ PairWindow pair_window(const DevConfig& cfg, uint32_t
   return w;
 }
 
+// pair_valid on (z, phi) with the phi test as two intervals, the second
+// empty unless the window wraps
+struct PairTest {
+  float zl, zh, a1, b1, a2, b2;
+};
+__device__ __forceinline__ PairTest pair_test(const PairWindow& w) {
+  const float inf = __int_as_float(0x7f800000);
+  PairTest t;
+  t.zl = w.zLow;
+  t.zh = w.zHigh;
+  t.a1 = w.phiLow;
+  t.b1 = w.wrap ? TRAX_PI_F : w.phiHigh;
+  t.a2 = w.wrap ? -TRAX_PI_F : inf;
+  t.b2 = w.wrap ? w.phiHigh : -inf;
+  return t;
+}
+__device__ __forceinline__ bool pair_ok(const PairTest& t, float2 h) {
+  return t.zl <= h.x && h.x <= t.zh && ((t.a1 <= h.y && h.y <= t.b1) || (t.a2 <= h.y && h.y <= t.b2));
+}
+
 __device__ __forceinline__ bool pair_valid(const PairWindow& w, float4 h) {
   bool valid = w.zLow <= h.z && h.z <= w.zHigh;
   const float actPhi = h.w;
@@ -196,6 +216,9 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
       }
       uint32_t written = 0;
       if (simple) {
+        // the common path tests (z, phi) pairs: 8 bytes per visited hit
+        const PairTest t = pair_test(w);
+        const float2* zphi = reinterpret_cast<const float2*>(hits) + 1;  // (z, phi) of hit j at zphi[2 j]
         for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
           uint32_t a1, b1, a2, b2;
           pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
@@ -204,12 +227,12 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
             lo0 = a2; hi0 = b2; lo1 = a1; hi1 = b1;
           }
           for (uint32_t j = lo0; j < hi0; ++j)
-            if (pair_valid(w, hits[j])) {
+            if (pair_ok(t, __ldg(zphi + 2 * (size_t)j))) {
               if (written < limit) out[written] = make_uint2(j, i);
               ++written;
             }
           for (uint32_t j = lo1; j < hi1; ++j)
-            if (pair_valid(w, hits[j])) {
+            if (pair_ok(t, __ldg(zphi + 2 * (size_t)j))) {
               if (written < limit) out[written] = make_uint2(j, i);
               ++written;
             }

@@ -64,18 +64,26 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
       uint32_t* slot = keep + (size_t)gid * TRAX_PRED_KEEP;
       uint32_t nStore = 0;
       const uint32_t zLo = min(w.zLoSec[0], w.zLoSec[1]), zHi = max(w.zHiSec[0], w.zHiSec[1]);
+      // the phi test as two intervals (the second empty unless the window
+      // wraps), and per row each variant's z interval (empty outside its rows)
+      const float inf = __int_as_float(0x7f800000);
+      const float pa1 = w.phiLow, pb1 = w.wrap ? TRAX_PI_F : w.phiHigh;
+      const float pa2 = w.wrap ? -TRAX_PI_F : inf, pb2 = w.wrap ? w.phiHigh : -inf;
+      const float2* zphi = reinterpret_cast<const float2*>(hits) + 1;  // (z, phi) of hit j at zphi[2 j]
       for (uint32_t zs = zLo; zs < zHi; ++zs) {
         const bool in0 = zs >= w.zLoSec[0] && zs < w.zHiSec[0];
         const bool in1 = zs >= w.zLoSec[1] && zs < w.zHiSec[1];
+        const float zl0 = in0 ? w.zLow[0] : inf, zh0 = in0 ? w.zHigh[0] : -inf;
+        const float zl1 = in1 ? w.zLow[1] : inf, zh1 = in1 ? w.zHigh[1] : -inf;
         uint32_t a[2], b[2];
         pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
 #pragma unroll
         for (int part = 0; part < 2; ++part) {
           for (uint32_t j = a[part]; j < b[part]; ++j) {
-            const float4 h = hits[j];
-            if (!pred_phi_ok(w, h.w)) continue;
-            count += (in0 && w.zLow[0] <= h.z && h.z <= w.zHigh[0]);
-            if (in1 && w.zLow[1] <= h.z && h.z <= w.zHigh[1]) {
+            const float2 h = __ldg(zphi + 2 * (size_t)j);
+            const bool phiOk = (pa1 <= h.y && h.y <= pb1) || (pa2 <= h.y && h.y <= pb2);
+            count += (phiOk && zl0 <= h.x && h.x <= zh0);
+            if (phiOk && zl1 <= h.x && h.x <= zh1) {
               if (nStore < TRAX_PRED_KEEP) slot[nStore] = j;
               ++nStore;
             }
