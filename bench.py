@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: autotuned)")
     p.add_argument("--no-tune", action="store_true", help="skip the autotuner (grid of the workload, default blocks)")
     p.add_argument("--tune-cache", default=None, help="JSON cache file of the autotuner")
+    p.add_argument("--blocks", default=None,
+                   help="block sizes of the pair, prediction and filter kernels, e.g. 256,64,256 (skips their tuning)")
     return p.parse_args()
 
 
@@ -172,7 +174,7 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells):
 # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # same chain on the first 300 events of the workload; a full launch scales
 # them by its units (traffic grows with pairs, candidates and hits).
-TRAFFIC_PER_UNIT = {"predict_count": ("pairs", 32.4), "filter": ("candidates", 28.5), "grid_build": ("hits", 124.2)}
+TRAFFIC_PER_UNIT = {"predict_count": ("pairs", 32.3), "filter": ("candidates", 25.7), "grid_build": ("hits", 111.0)}
 
 
 def kernel_traffic(name, st, n_hits):
@@ -279,7 +281,9 @@ def run_ours(args, ranks):
     ctx = capi.Context(device)
     ctx.upload(batch)
     tune = None
-    if not args.no_tune:
+    if args.blocks:
+        ctx.set_block_sizes(*(int(v) for v in args.blocks.split(",")))
+    elif not args.no_tune:
         # grid searched unless --grid fixes it; block sizes always
         tune = ctx.autotune(cache_path=args.tune_cache, search_grid=not args.grid)
         batch.n_z, batch.n_phi = tune["n_z"], tune["n_phi"]
