@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--plain-events", type=int, default=48)
     p.add_argument("--cpu-sample", type=int, default=128)
     p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-contexts", type=int, default=4,
+                   help="contexts (each with its own stream and host thread) that overlap copies with kernels")
     p.add_argument("--no-plain", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-parity", action="store_true")
@@ -406,11 +408,11 @@ def run_ours(args, ranks):
         serial = {"value": round(ranks.sum(float(batch.n_events * len(e2e_times))) / ranks.max(sum(e2e_times)), 2),
                   "unit": "events/s", "note": "one context: upload, replay and download one after the other"}
 
-        # two contexts on their own streams and host threads: one batch's
-        # copies run while the other's kernels do (copy engines and SMs overlap)
+        # several contexts on their own streams and host threads: one batch's
+        # copies run while the others' kernels do (copy engines and SMs overlap)
         shape_now = ctx.launch_config()
         pipes = []
-        for _ in range(2):
+        for _ in range(max(args.e2e_contexts, 1)):
             c2 = capi.Context(device)
             c2.upload(pbatch)
             c2.set_grid(shape_now["n_z"], shape_now["n_phi"])
@@ -452,14 +454,15 @@ def run_ours(args, ranks):
             raise RuntimeError("pipelined contexts returned different triplets")
         for c2, _o in pipes:
             c2.close()
-        n_steps = 2 * steps_each
+        n_steps = len(pipes) * steps_each
         e2e_t = ranks.max(dt)
         e2e_events = ranks.sum(float(batch.n_events * n_steps))
         result["e2e"] = {"value": round(e2e_events / e2e_t, 2), "unit": "events/s", "h2d_bytes_per_step": bi,
                          "d2h_bytes_per_step": bo, "steps": n_steps,
+                         "contexts": len(pipes),
                          "note": "page-locked host arrays (trax_host_alloc); every step uploads the batch, replays "
-                                 "the chain and downloads triplets and tracks; two contexts on their own streams "
-                                 "and host threads overlap one step's copies with the other's kernels; wall clock",
+                                 "the chain and downloads triplets and tracks; contexts on their own streams and "
+                                 "host threads overlap one step's copies with the others' kernels; wall clock",
                          "serial": serial}
         pg_times, _ = e2e_run(batch, False)
         result["e2e_pageable"] = {"value": round(ranks.sum(float(batch.n_events * len(pg_times)))

@@ -250,6 +250,41 @@ def test_pileup_stress_event_matches_oracle(ctx, oracle_lib):
     compare(ctx.results(), ref)
 
 
+def test_grid_build_hit_arrays_outside_shared_memory(ctx, oracle_lib):
+    """The grid build keeps each hit's cell, phi and slot in shared memory
+    when the largest layer fits beside the cell counters.  Two ways past it:
+    a grid whose counters leave no room (every layer in global scratch), and
+    a replay of a graph captured for a smaller largest layer (the layers
+    that do not fit fall back one by one)."""
+    batch = events.generate(1, n_events=20)
+    lh = batch.layer_hits
+    # the event whose first two layers together outnumber every single layer
+    e = int(np.argmax(lh[:, 0] + lh[:, 1]))
+    assert lh[e, 0] + lh[e, 1] > lh.max()
+    merged = events.generate(1, n_events=20)
+    in_e = merged.event == e
+    merged.layer = np.where(in_e & (merged.layer == 2), 1, merged.layer).astype(merged.layer.dtype)
+    mlh = merged.layer_hits.copy()
+    mlh[e, 0] += mlh[e, 1]
+    mlh[e, 1] = 0
+    merged = events._assemble({k: getattr(merged, k) for k in ("x", "y", "z", "layer", "det_id", "hit_id", "event")},
+                              mlh, merged)
+    ref = oracle_lib.run(merged)[0]
+    ctx.upload(batch)
+    ctx.seed_batch(use_graph=True)
+    ctx.upload(merged)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+    # 401 x 129 cells: 207 KB of counters, no room for a layer of 2747 hits
+    dense = events.generate(2, n_events=2, seed=4)
+    dense.n_z, dense.n_phi = 400, 128
+    assert dense.layer_hits.max() * 12 > 227 * 1024 - 256 - 401 * 129 * 4
+    ref = oracle_lib.run(dense)[0]
+    ctx.upload(dense)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
 def test_capacity_overflow_recalibrates(ctx, oracle_lib):
     """A batch of the same shape but far denser hits overflows the capacities
     calibrated on the first: the call recalibrates, recaptures and returns the

@@ -122,6 +122,7 @@ struct trax_ctx {
   // bookkeeping
   DevBuf scanScratch, slots;
   uint32_t* hSlots = nullptr;  // pinned copy of the slots
+  uint32_t maxLayerHits = 0;   // most hits of one (event, layer) in the uploaded batch
   // sizes of the last run
   uint64_t nTasks = 0, nPairs = 0, nCands = 0, nT = 0, nLinks = 0, nConn = 0, nNonConn = 0, nTracks = 0;
   uint64_t pairSent = 0, candSent = 0;
@@ -392,7 +393,8 @@ int stage_grid(trax_ctx* c, Mode mode) {
   sc.perm = ptr<uint32_t>(c->sc_perm);
   sc.counts = ptr<uint32_t>(c->sc_counts);
   KBEG(TK_GRID);
-  CK(grid_build(c->cfg, in, ptr<uint32_t>(c->grid), dev_hits(c), sc, dev_err(c), c->st, &c->launches));
+  CK(grid_build(c->cfg, in, ptr<uint32_t>(c->grid), dev_hits(c), sc, c->maxLayerHits, dev_err(c), c->st,
+                &c->launches));
   KEND(TK_GRID);
   return TRAX_OK;
 }
@@ -994,6 +996,7 @@ int trax_upload_hits(trax_ctx* c, const trax_hits_soa* h, uint32_t n_hits, const
   if (n_layers == 0 || n_layers > TRAX_MAX_LAYERS) return fail(c, TRAX_ERR_ARG, "invalid number of layers");
   // the supplements must describe the hits contiguously (HitCollection.cpp:120-133)
   uint64_t pos = 0;
+  uint32_t maxLayer = 0;
   for (uint32_t e = 0; e < n_events; ++e) {
     if (event_offsets[e] != pos) return fail(c, TRAX_ERR_ARG, "event offsets are not contiguous");
     uint64_t lpos = 0;
@@ -1001,6 +1004,7 @@ int trax_upload_hits(trax_ctx* c, const trax_hits_soa* h, uint32_t n_hits, const
       const size_t k = (size_t)e * n_layers + l;
       if (layer_offsets[k] != lpos) return fail(c, TRAX_ERR_ARG, "layer offsets are not contiguous");
       lpos += layer_hits[k];
+      maxLayer = std::max(maxLayer, layer_hits[k]);
     }
     pos += lpos;
   }
@@ -1026,6 +1030,7 @@ int trax_upload_hits(trax_ctx* c, const trax_hits_soa* h, uint32_t n_hits, const
   c->E = n_events;
   c->L = n_layers;
   c->nHits = n_hits;
+  c->maxLayerHits = maxLayer;
   c->haveHits = true;
   c->stage = 0;
   return TRAX_OK;

@@ -7,7 +7,9 @@
 // global scan of the reference reduces to base + local scan), places every
 // hit at a STABLE slot (hits keep their input order inside a cell, one of
 // the orders the reference's atomic_inc can produce) and finally gathers the
-// seven hit columns into cell order with coalesced stores.  It also writes
+// seven hit columns into cell order with coalesced stores.  The cell, phi and
+// slot of every hit stay in shared memory next to the counters when the
+// largest layer fits, else in global scratch.  It also writes
 // the packed (x, y, z, phi) array the candidate loops read with one 16-byte
 // load, phi being the same atan2 the cell assignment used.
 #include "trax_kernels.h"
@@ -21,10 +23,16 @@ constexpr int GRID_WARPS = GRID_THREADS / 32;
 // cell counters live in shared memory up to TRAX_GRID_SMEM_CELLS cells (208 KB,
 // one CTA per SM at the largest grids); larger grids count in global memory
 constexpr uint32_t GRID_SMEM_CELLS = TRAX_GRID_SMEM_CELLS;
+// dynamic shared memory a CTA may use: the counters plus, when they fit, the
+// cell, phi and slot of each of the layer's hits (12 bytes per hit)
+constexpr size_t GRID_SMEM_MAX = 227 * 1024 - 256;
 
+// The per-hit cell, phi and slot arrays are in shared memory after the
+// counters when the layer has at most maxHits hits (the room the launch
+// gave them), otherwise in the global scratch arrays.
 __global__ void __launch_bounds__(GRID_THREADS)
     grid_kernel(DevConfig cfg, GridInput in, uint32_t* __restrict__ grid, DevHits out, GridScratch sc,
-                uint32_t* err, int useSmem) {
+                uint32_t* err, int useSmem, uint32_t maxHits) {
   extern __shared__ uint32_t smem[];
   __shared__ uint32_t s_warpSum[GRID_WARPS];
   const uint32_t task = blockIdx.x;  // event * L + layer
@@ -33,6 +41,11 @@ __global__ void __launch_bounds__(GRID_THREADS)
   const uint32_t n = in.layerHits[task];
   const uint32_t base = in.eventOffsets[e] + in.layerOffsets[task];
   uint32_t* cnt = useSmem ? smem : sc.counts + (size_t)task * C;
+  // per-hit arrays, indexed by the hit's position i in the layer
+  const bool inSmem = useSmem && n <= maxHits;
+  uint32_t* cellOf = inSmem ? smem + C : sc.cell + base;
+  float* phiOf = inSmem ? reinterpret_cast<float*>(smem + C + maxHits) : sc.phi + base;
+  uint32_t* perm = inSmem ? smem + C + 2 * maxHits : sc.perm + base;
   const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
 
   for (uint32_t c = tid; c < C; c += GRID_THREADS) cnt[c] = 0u;
@@ -51,8 +64,8 @@ __global__ void __launch_bounds__(GRID_THREADS)
       phiSector = min(phiSector, cfg.nP);
     }
     const uint32_t cell = zSector * (cfg.nP + 1) + phiSector;
-    sc.cell[k] = cell;
-    sc.phi[k] = phi;
+    cellOf[i] = cell;
+    phiOf[i] = phi;
     atomicAdd(&cnt[cell], 1u);
   }
   __syncthreads();
@@ -90,23 +103,19 @@ __global__ void __launch_bounds__(GRID_THREADS)
   //    input index -- the stable order, one of the orders the reference's
   //    atomic_inc can produce.  After the atomics cnt[c] is the end of cell c,
   //    and so the start of cell c + 1.
-  for (uint32_t i = tid; i < n; i += GRID_THREADS) {
-    const uint32_t cell = sc.cell[base + i];
-    sc.perm[base + atomicAdd(&cnt[cell], 1u)] = i;
-  }
+  for (uint32_t i = tid; i < n; i += GRID_THREADS) perm[atomicAdd(&cnt[cellOf[i]], 1u)] = i;
   __syncthreads();
   for (uint32_t c = tid; c < C; c += GRID_THREADS) {
     const uint32_t lo = c ? cnt[c - 1] : 0u, hi = cnt[c];
     if (hi - lo < 2) continue;
-    uint32_t* p = sc.perm + base;
     for (uint32_t a = lo + 1; a < hi; ++a) {  // insertion sort: cells hold a few hits
-      const uint32_t v = p[a];
+      const uint32_t v = perm[a];
       uint32_t b = a;
-      while (b > lo && p[b - 1] > v) {
-        p[b] = p[b - 1];
+      while (b > lo && perm[b - 1] > v) {
+        perm[b] = perm[b - 1];
         --b;
       }
-      p[b] = v;
+      perm[b] = v;
     }
   }
   __syncthreads();
@@ -114,7 +123,8 @@ __global__ void __launch_bounds__(GRID_THREADS)
   // 4. gather into cell order (gridStore, GridBuilder.h:243-253)
   for (uint32_t s = tid; s < n; s += GRID_THREADS) {
     const uint32_t dst = base + s;
-    const uint32_t src = base + sc.perm[dst];
+    const uint32_t i = perm[s];
+    const uint32_t src = base + i;
     const float x = in.x[src], y = in.y[src], z = in.z[src];
     out.x[dst] = x;
     out.y[dst] = y;
@@ -124,7 +134,7 @@ __global__ void __launch_bounds__(GRID_THREADS)
     out.hid[dst] = in.hid[src];
     out.evt[dst] = in.evt[src];
     out.orig[dst] = src;
-    out.xyzp[dst] = make_float4(x, y, z, sc.phi[src]);
+    out.xyzp[dst] = make_float4(x, y, z, phiOf[i]);
   }
 }
 
@@ -155,17 +165,19 @@ cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStre
 }
 
 cudaError_t grid_prepare(int) {
-  return cudaFuncSetAttribute(grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)(GRID_SMEM_CELLS * sizeof(uint32_t)));
+  return cudaFuncSetAttribute(grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
 }
 
 cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid, DevHits out, GridScratch sc,
-                       uint32_t* err, cudaStream_t st, uint32_t* launches) {
+                       uint32_t maxLayerHits, uint32_t* err, cudaStream_t st, uint32_t* launches) {
   const uint32_t tasks = cfg.E * cfg.L;
   if (tasks == 0) return cudaSuccess;
   const int useSmem = cfg.C <= GRID_SMEM_CELLS ? 1 : 0;
-  const size_t smemBytes = useSmem ? (size_t)cfg.C * sizeof(uint32_t) : 0;
-  grid_kernel<<<tasks, GRID_THREADS, smemBytes, st>>>(cfg, in, grid, out, sc, err, useSmem);
+  const size_t counterBytes = useSmem ? (size_t)cfg.C * sizeof(uint32_t) : 0;
+  const size_t hitBytes = (size_t)maxLayerHits * 3 * sizeof(uint32_t);
+  const bool hitsFit = useSmem && counterBytes + hitBytes <= GRID_SMEM_MAX;
+  grid_kernel<<<tasks, GRID_THREADS, counterBytes + (hitsFit ? hitBytes : 0), st>>>(
+      cfg, in, grid, out, sc, err, useSmem, hitsFit ? maxLayerHits : 0u);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

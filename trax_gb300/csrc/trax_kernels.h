@@ -45,7 +45,8 @@ struct GridScratch {
 };
 
 cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid, DevHits out,
-                       GridScratch scratch, uint32_t* err, cudaStream_t st, uint32_t* launches);
+                       GridScratch scratch, uint32_t maxLayerHits, uint32_t* err, cudaStream_t st,
+                       uint32_t* launches);
 cudaError_t grid_prepare(int device);  // one-time kernel attributes
 // hit collection = uploaded hits in input order (plus the packed xyz-phi array)
 cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStream_t st, uint32_t* launches);
