@@ -113,7 +113,7 @@ struct trax_ctx {
   // grid stage
   DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
   // pair stage
-  DevBuf segOuter, taskBase, taskCount, pairs, pairOffsets;
+  DevBuf segOuter, taskBase, taskCount, taskOrdered, pairs, pairOffsets;
   // prediction / filter
   DevBuf candCount, predWarps, predKeep, cands, candOffsets, flagWords, flagSums, h1, h2, h3, tripOffsets;
   // connectivity / fit / CA
@@ -414,10 +414,13 @@ int stage_pairs(trax_ctx* c, Mode mode) {
     maxTasks = c->nTasks;
   }
   ENSURE(taskCount, maxTasks + 1, 4);
+  ENSURE(taskOrdered, maxTasks + 1, 1);
   uint32_t* taskCount = ptr<uint32_t>(c->taskCount);
+  uint8_t* taskOrdered = ptr<uint8_t>(c->taskOrdered);
   KBEG(TK_PAIR_COUNT);
   CK(pair_tasks(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
-                maxTasks, taskCount, nullptr, 0, slot(c, S_PAIR_SENT), dev_err(c), c->st, &c->launches));
+                maxTasks, taskCount, taskOrdered, nullptr, 0, slot(c, S_PAIR_SENT), dev_err(c), c->st,
+                &c->launches));
   KEND(TK_PAIR_COUNT);
   RC(scan_publish(c, mode, taskCount, c->nTasks, mode == DEVICE ? nTasksDev : nullptr, maxTasks, S_PAIRS,
                   mode == DEVICE ? c->capPairs : NO_CAP));
@@ -429,8 +432,8 @@ int stage_pairs(trax_ctx* c, Mode mode) {
   ENSURE(pairs, maxPairs, 8);
   KBEG(TK_PAIR_EMIT);
   CK(pair_tasks(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
-                maxTasks, taskCount, ptr<uint2>(c->pairs), maxPairs, slot(c, S_PAIR_SENT), dev_err(c), c->st,
-                &c->launches));
+                maxTasks, taskCount, taskOrdered, ptr<uint2>(c->pairs), maxPairs, slot(c, S_PAIR_SENT), dev_err(c),
+                c->st, &c->launches));
   KEND(TK_PAIR_EMIT);
   CK(pair_offsets(c->cfg, taskBase, taskCount, ptr<uint32_t>(c->pairOffsets), c->st, &c->launches));
   return TRAX_OK;
@@ -699,6 +702,7 @@ int size_device_buffers(trax_ctx* c) {
   c->capTracks = with_headroom(c->nTracks);
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   ENSURE(taskCount, c->capTasks + 1, 4);
+  ENSURE(taskOrdered, c->capTasks + 1, 1);
   ENSURE(pairs, c->capPairs, 8);
   ENSURE(candCount, c->capPairs + 1, 4);
   ENSURE(predWarps, (c->capPairs + 31) / 32 + 1, 4);
@@ -898,7 +902,7 @@ void trax_destroy(trax_ctx* c) {
   DevBuf* bufs[] = {&c->in_x, &c->in_y, &c->in_z, &c->in_layer, &c->in_det, &c->in_hid, &c->in_evt, &c->evOff,
                     &c->layHits, &c->layOff, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
-                    &c->segOuter, &c->taskBase, &c->taskCount, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
+                    &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,

@@ -134,6 +134,32 @@ __device__ __forceinline__ void pair_row_parts(const PairWindow& w, const uint32
   }
 }
 
+// One row of the ordering check: its two ranges are disjoint and both start
+// at or after prevEnd, the end of everything before (advanced here).
+__device__ __forceinline__ bool rows_in_order(uint32_t a1, uint32_t b1, uint32_t a2, uint32_t b2,
+                                              uint32_t& prevEnd) {
+  const bool n1 = a1 < b1, n2 = a2 < b2;
+  bool ok = true;
+  if (n1 && n2) {
+    if (b2 <= a1) {
+      ok = a2 >= prevEnd;
+      prevEnd = b1;
+    } else if (b1 <= a2) {
+      ok = a1 >= prevEnd;
+      prevEnd = b2;
+    } else {
+      ok = false;
+    }
+  } else if (n1) {
+    ok = a1 >= prevEnd;
+    prevEnd = b1;
+  } else if (n2) {
+    ok = a2 >= prevEnd;
+    prevEnd = b2;
+  }
+  return ok;
+}
+
 __device__ __forceinline__ uint32_t find_segment(const uint32_t* taskBase, uint32_t S, uint32_t k) {
   // largest s with taskBase[s] <= k
   uint32_t lo = 0, hi = S;  // taskBase[S] > k
@@ -162,8 +188,8 @@ template <bool EMIT>
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     pair_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                 const uint32_t* __restrict__ segOuter, const uint32_t* __restrict__ taskBase,
-                const uint32_t* __restrict__ nTasksDev, uint32_t* taskCount, uint2* pairs, uint32_t capPairs,
-                uint32_t* sentinels, uint32_t* err) {
+                const uint32_t* __restrict__ nTasksDev, uint32_t* taskCount, uint8_t* orderedRows, uint2* pairs,
+                uint32_t capPairs, uint32_t* sentinels, uint32_t* err) {
   const uint32_t S = cfg.E * cfg.nLT;
   const uint32_t nTasks = *nTasksDev;
   const uint32_t C = cfg.C, nP = cfg.nP;
@@ -176,44 +202,26 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     const uint32_t* lG1 = grid + ((size_t)e * cfg.L + (cfg.layer1[p] - 1)) * C;
     if (!EMIT) {
       uint32_t nFound = 0;
+      // whether the rows' ranges are disjoint and ascending, for the store
+      bool simple = true;
+      uint32_t prevEnd = 0;
       for (uint32_t zs = w.zLowSector; zs < w.zHighSector; ++zs) {
         uint32_t a1, b1, a2, b2;
         pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
+        if (simple) simple = rows_in_order(a1, b1, a2, b2, prevEnd);
         for (uint32_t j = a1; j < b1; ++j) nFound += pair_valid(w, hits[j]);
         for (uint32_t j = a2; j < b2; ++j) nFound += pair_valid(w, hits[j]);
       }
       taskCount[k] = nFound;
+      orderedRows[k] = simple ? 1 : 0;
     } else {
       const uint32_t pos0 = taskCount[k];
       uint32_t limit = taskCount[k + 1] - pos0;
       if (pos0 >= capPairs) limit = 0;
       else if (limit > capPairs - pos0) limit = capPairs - pos0;
       uint2* out = pairs + pos0;
-      // ordering check: ranges disjoint and ascending
-      bool simple = true;
-      uint32_t prevEnd = 0;
-      for (uint32_t zs = w.zLowSector; zs < w.zHighSector && simple; ++zs) {
-        uint32_t a1, b1, a2, b2;
-        pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
-        const bool n1 = a1 < b1, n2 = a2 < b2;
-        if (n1 && n2) {
-          if (b2 <= a1) {
-            simple = a2 >= prevEnd;
-            prevEnd = b1;
-          } else if (b1 <= a2) {
-            simple = a1 >= prevEnd;
-            prevEnd = b2;
-          } else {
-            simple = false;
-          }
-        } else if (n1) {
-          simple = a1 >= prevEnd;
-          prevEnd = b1;
-        } else if (n2) {
-          simple = a2 >= prevEnd;
-          prevEnd = b2;
-        }
-      }
+      // the count pass checked the ordering of the ranges
+      const bool simple = orderedRows[k] != 0;
       uint32_t written = 0;
       if (simple) {
         // the common path tests (z, phi) pairs: 8 bytes per visited hit
@@ -287,18 +295,18 @@ cudaError_t pair_segments(const DevConfig& cfg, const uint32_t* grid, uint32_t* 
 
 cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint32_t* segOuter,
                        const uint32_t* taskBase, const uint32_t* nTasksDev, uint64_t maxTasks, uint32_t* taskCount,
-                       uint2* pairs, uint64_t capPairs, uint32_t* sentinels, uint32_t* err, cudaStream_t st,
-                       uint32_t* launches) {
+                       uint8_t* orderedRows, uint2* pairs, uint64_t capPairs, uint32_t* sentinels, uint32_t* err,
+                       cudaStream_t st, uint32_t* launches) {
   const uint32_t cap = capPairs > 0xffffffffull ? 0xffffffffu : (uint32_t)capPairs;
   if (emit && maxTasks == 0) return cudaSuccess;
   const int threads = (int)cfg.pairThreads;
   const int blocks = grid_for(maxTasks + 1, threads);
   if (emit)
     pair_kernel<true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
-                                                       taskCount, pairs, cap, sentinels, err);
+                                                       taskCount, orderedRows, pairs, cap, sentinels, err);
   else
     pair_kernel<false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
-                                                        taskCount, pairs, cap, sentinels, err);
+                                                        taskCount, orderedRows, pairs, cap, sentinels, err);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

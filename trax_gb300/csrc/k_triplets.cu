@@ -206,44 +206,55 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     filter_kernel(DevConfig cfg, const float4* __restrict__ hits, const uint32_t* __restrict__ hitLayer,
                   const uint2* __restrict__ pairs, const uint2* __restrict__ cands, const uint32_t* nCandsDev,
                   uint32_t* masks, uint32_t* warpSums, uint32_t* nWordsOut) {
-  __shared__ uint32_t s_queue[TRAX_MAX_TUNED_THREADS];
-  __shared__ uint8_t s_flag[TRAX_MAX_TUNED_THREADS];
-  __shared__ uint32_t s_n;
+  constexpr uint32_t WORDS = 32;  // a warp takes 32 words = 1024 candidates at a time
+  __shared__ uint32_t s_queue[TRAX_MAX_TUNED_THREADS / 32][64];
+  __shared__ uint32_t s_bits[TRAX_MAX_TUNED_THREADS / 32][WORDS];
   const uint32_t n = *nCandsDev;
-  const uint32_t T = blockDim.x, lane = threadIdx.x & 31u;
-  for (uint32_t g0 = blockIdx.x * T; g0 < n; g0 += gridDim.x * T) {
-    if (threadIdx.x == 0) s_n = 0;
-    s_flag[threadIdx.x] = 0;
-    __syncthreads();
-    const uint32_t g = g0 + threadIdx.x;
-    bool pass = false;
-    if (g < n) {
-      const uint2 c = cands[g];
-      if (c.y != TRAX_SENTINEL) {  // a slot the reference never wrote fails
-        const uint2 pr = pairs[c.x];
-        pass = filter_dphi(cfg.dPhiCut[hitLayer[pr.x] - 1], hits[pr.x], hits[pr.y], hits[c.y]);
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+  uint32_t* queue = s_queue[warp];
+  uint32_t* bits = s_bits[warp];
+  auto rest = [&](uint32_t g0, uint32_t g) {
+    const uint2 c = cands[g];
+    const uint2 pr = pairs[c.x];
+    if (filter_rest(cfg, hitLayer[pr.x] - 1, hits[pr.x], hits[pr.y], hits[c.y]))
+      atomicOr(&bits[(g - g0) >> 5], 1u << (g & 31u));
+  };
+  for (uint32_t g0 = (blockIdx.x * (blockDim.x >> 5) + warp) * (WORDS * 32); g0 < n; g0 += warps * WORDS * 32) {
+    bits[lane] = 0u;
+    uint32_t queued = 0;  // warp-uniform
+    __syncwarp();
+    for (uint32_t k = 0; k < WORDS; ++k) {
+      const uint32_t g = g0 + k * 32 + lane;
+      bool pass = false;
+      if (g < n) {
+        const uint2 c = cands[g];
+        if (c.y != TRAX_SENTINEL) {  // a slot the reference never wrote fails
+          const uint2 pr = pairs[c.x];
+          pass = filter_dphi(cfg.dPhiCut[hitLayer[pr.x] - 1], hits[pr.x], hits[pr.y], hits[c.y]);
+        }
+      }
+      const uint32_t ballot = __ballot_sync(0xffffffffu, pass);
+      if (pass) queue[queued + __popc(ballot & lanemask_lt())] = g;
+      queued += __popc(ballot);
+      __syncwarp();
+      if (queued >= 32) {  // a full round of the remaining tests
+        rest(g0, queue[lane]);
+        __syncwarp();
+        if (lane < queued - 32) queue[lane] = queue[32 + lane];
+        queued -= 32;
+        __syncwarp();
       }
     }
-    const uint32_t ballot = __ballot_sync(0xffffffffu, pass);
-    uint32_t slot0 = 0;
-    if (lane == 0 && ballot) slot0 = atomicAdd(&s_n, (uint32_t)__popc(ballot));
-    slot0 = __shfl_sync(0xffffffffu, slot0, 0);
-    if (pass) s_queue[slot0 + __popc(ballot & lanemask_lt())] = threadIdx.x;
-    __syncthreads();
-    const uint32_t m = s_n;
-    for (uint32_t q = threadIdx.x; q < m; q += T) {
-      const uint32_t t = s_queue[q];
-      const uint2 c = cands[g0 + t];
-      const uint2 pr = pairs[c.x];
-      s_flag[t] = filter_rest(cfg, hitLayer[pr.x] - 1, hits[pr.x], hits[pr.y], hits[c.y]) ? 1 : 0;
+    if (lane < queued) rest(g0, queue[lane]);
+    __syncwarp();
+    const uint32_t word = (g0 >> 5) + lane;
+    if (g0 + lane * 32 < n) {
+      const uint32_t b = bits[lane];
+      masks[word] = b;
+      warpSums[word] = (uint32_t)__popc(b);
     }
-    __syncthreads();
-    const uint32_t word = __ballot_sync(0xffffffffu, s_flag[threadIdx.x] != 0);
-    if (lane == 0 && g < n) {
-      masks[g >> 5] = word;
-      warpSums[g >> 5] = (uint32_t)__popc(word);
-    }
-    __syncthreads();
+    __syncwarp();
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const uint32_t nW = (n + 31u) >> 5;

@@ -57,10 +57,13 @@ cudaError_t pair_segments(const DevConfig& cfg, const uint32_t* grid, uint32_t* 
                           cudaStream_t st, uint32_t* launches);
 // Count (emit == false) or store (emit == true) pairs of every outer-hit task.
 // taskBase[S+1] is the exclusive scan of segCount; nTasksDev = &taskBase[S].
+// orderedRows[k]: whether task k's visit ranges are disjoint and ascending
+// (written by the count pass, read by the store pass)
 cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits,
                        const uint32_t* segOuter, const uint32_t* taskBase, const uint32_t* nTasksDev,
-                       uint64_t maxTasks, uint32_t* taskCount, uint2* pairs, uint64_t capPairs,
-                       uint32_t* sentinelCount, uint32_t* err, cudaStream_t st, uint32_t* launches);
+                       uint64_t maxTasks, uint32_t* taskCount, uint8_t* orderedRows, uint2* pairs,
+                       uint64_t capPairs, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
+                       uint32_t* launches);
 // pairOffsets[s+1] = first pair of segment s+1 (Pairing::pairingOffsets)
 cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const uint32_t* pairStart,
                          uint32_t* pairOffsets, cudaStream_t st, uint32_t* launches);
