@@ -192,16 +192,18 @@ __global__ void predict_offsets_kernel(uint32_t S, const uint32_t* __restrict__ 
   }
 }
 
-// The flags in two steps per block of candidates: every candidate takes the
-// dphi test, which rejects most of them (two atan2); the block queues the
-// survivors and its threads then run the dtheta / TIP / curvature tests on
-// the queue, densely, instead of leaving rejected lanes idle beside them.
-// The flag is the AND of filterCount's four predicates (TripletThetaPhiFilter.h:65-154).
-// filterPopCount + PrefixSum run on words of 32 flags: each warp of 32
-// consecutive candidates stores its flags as one ballot mask and their
-// number in warpSums (+1 slot zeroed, the number of words to *nWordsOut),
-// and only those sums are scanned; a triplet's position is its word's
-// scanned sum plus the flags set below it in the word.
+// The flags in two steps, each warp on its own (no block barriers): a warp
+// takes 1024 consecutive candidates, 32 at a time; every candidate takes the
+// dphi test, which rejects most of them (two atan2), and the survivors go to
+// the warp's queue in shared memory.  Whenever the queue holds 32 the warp
+// runs the dtheta / TIP / curvature tests on them with every lane busy, and
+// it empties the queue at the end of its 1024.  The flag is the AND of
+// filterCount's four predicates (TripletThetaPhiFilter.h:65-154).
+// filterPopCount + PrefixSum run on words of 32 flags: the flags of 32
+// consecutive candidates are one word of masks, the number set goes to
+// warpSums (+1 slot zeroed, the number of words to *nWordsOut), and only
+// those sums are scanned; a triplet's position is its word's scanned sum
+// plus the flags set below it in the word.
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     filter_kernel(DevConfig cfg, const float4* __restrict__ hits, const uint32_t* __restrict__ hitLayer,
                   const uint2* __restrict__ pairs, const uint2* __restrict__ cands, const uint32_t* nCandsDev,
