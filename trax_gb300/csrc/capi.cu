@@ -68,6 +68,7 @@ enum Slot {
   S_TRACKS,
   S_PRED_WARPS,
   S_FLAG_WORDS,
+  S_CONN_WORDS,
   S_N
 };
 
@@ -117,7 +118,7 @@ struct trax_ctx {
   // prediction / filter
   DevBuf candCount, predWarps, predKeep, cands, candOffsets, flagWords, flagSums, h1, h2, h3, tripOffsets;
   // connectivity / fit / CA
-  DevBuf eta, segOf, segStart, linkCount, cflags, basis, follower, connS, nonConnS, connIdx, nonConnIdx, pt;
+  DevBuf eta, segOf, segStart, linkCount, linkRun, cflags, basis, follower, connS, nonConnS, connW, nonConnW, connIdx, nonConnIdx, pt;
   DevBuf states, inStart, inCursor, inList, best, isBest, handlers, tracks;
   // bookkeeping
   DevBuf scanScratch, slots;
@@ -530,9 +531,13 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
   ENSURE(segOf, maxT, 4);
   ENSURE(segStart, S + 1, 4);
   ENSURE(linkCount, maxT + 1, 4);
+  ENSURE(linkRun, maxT + 1, 4);
   ENSURE(cflags, maxT + 1, 4);
-  ENSURE(connS, maxT + 1, 4);
-  ENSURE(nonConnS, maxT + 1, 4);
+  const uint64_t maxTW = (maxT + 31) / 32;
+  ENSURE(connS, maxTW + 1, 4);
+  ENSURE(nonConnS, maxTW + 1, 4);
+  ENSURE(connW, maxTW + 1, 4);
+  ENSURE(nonConnW, maxTW + 1, 4);
   ENSURE(connIdx, maxT, 4);
   ENSURE(nonConnIdx, maxT, 4);
   TripletView tv = triplets(c, maxT);
@@ -542,8 +547,8 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
   uint32_t* linkCount = ptr<uint32_t>(c->linkCount);
   KBEG(TK_CONN_COUNT);
   CK(connectivity_tasks(c->cfg, false, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
-                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), nullptr, nullptr, 0,
-                        c->sortedSegments, c->st, &c->launches));
+                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), ptr<uint32_t>(c->linkRun),
+                        nullptr, nullptr, 0, c->sortedSegments, c->st, &c->launches));
   KEND(TK_CONN_COUNT);
   RC(scan_publish(c, mode, linkCount, c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_LINKS,
                   mode == DEVICE ? c->capLinks : NO_CAP));
@@ -558,17 +563,22 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
   ENSURE(follower, maxLinks, 4);
   KBEG(TK_CONN_EMIT);
   CK(connectivity_tasks(c->cfg, true, dev_hits(c), tv, ptr<float>(c->eta), ptr<uint32_t>(c->tripOffsets),
-                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), ptr<uint32_t>(c->basis),
-                        ptr<uint32_t>(c->follower), maxLinks, c->sortedSegments, c->st, &c->launches));
+                        ptr<uint32_t>(c->segStart), linkCount, ptr<uint32_t>(c->cflags), ptr<uint32_t>(c->linkRun),
+                        ptr<uint32_t>(c->basis), ptr<uint32_t>(c->follower), maxLinks, c->sortedSegments, c->st,
+                        &c->launches));
   KEND(TK_CONN_EMIT);
-  CK(connectable_streams(ptr<uint32_t>(c->cflags), nTDev, maxT, ptr<uint32_t>(c->connS), ptr<uint32_t>(c->nonConnS),
-                         c->st, &c->launches));
-  RC(scan_publish(c, mode, ptr<uint32_t>(c->connS), c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_CONN, NO_CAP));
-  RC(scan_publish(c, mode, ptr<uint32_t>(c->nonConnS), c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_NONCONN,
-                  NO_CAP));
-  CK(compact_indices(ptr<uint32_t>(c->connS), nTDev, maxT, ptr<uint32_t>(c->connIdx), maxT, c->st, &c->launches));
-  CK(compact_indices(ptr<uint32_t>(c->nonConnS), nTDev, maxT, ptr<uint32_t>(c->nonConnIdx), maxT, c->st,
-                     &c->launches));
+  // the two Q9 streams as words of 32 flags; the scans run over the words' counts
+  CK(connectable_words(ptr<uint32_t>(c->cflags), nTDev, maxT, ptr<uint32_t>(c->connW), ptr<uint32_t>(c->connS),
+                       ptr<uint32_t>(c->nonConnW), ptr<uint32_t>(c->nonConnS), slot(c, S_CONN_WORDS), c->st,
+                       &c->launches));
+  const uint64_t nTW = (c->nT + 31) / 32;
+  const uint32_t* nTWDev = mode == DEVICE ? slot(c, S_CONN_WORDS) : nullptr;
+  RC(scan_publish(c, mode, ptr<uint32_t>(c->connS), nTW, nTWDev, maxTW, S_CONN, NO_CAP));
+  RC(scan_publish(c, mode, ptr<uint32_t>(c->nonConnS), nTW, nTWDev, maxTW, S_NONCONN, NO_CAP));
+  CK(compact_words(ptr<uint32_t>(c->connW), ptr<uint32_t>(c->connS), nTDev, maxT, ptr<uint32_t>(c->connIdx), maxT,
+                   c->st, &c->launches));
+  CK(compact_words(ptr<uint32_t>(c->nonConnW), ptr<uint32_t>(c->nonConnS), nTDev, maxT, ptr<uint32_t>(c->nonConnIdx),
+                   maxT, c->st, &c->launches));
   if (mode == SYNCED) {
     RC(read_slots(c));
     c->nConn = c->hSlots[S_CONN];
@@ -712,8 +722,9 @@ int size_device_buffers(trax_ctx* c) {
   ENSURE(flagSums, (c->capCands + 31) / 32 + 1, 4);
   ENSURE(h1, c->capT, 4); ENSURE(h2, c->capT, 4); ENSURE(h3, c->capT, 4);
   ENSURE(eta, c->capT, 4); ENSURE(segOf, c->capT, 4); ENSURE(segStart, S + 1, 4);
-  ENSURE(linkCount, c->capT + 1, 4); ENSURE(cflags, c->capT + 1, 4);
-  ENSURE(connS, c->capT + 1, 4); ENSURE(nonConnS, c->capT + 1, 4);
+  ENSURE(linkCount, c->capT + 1, 4); ENSURE(linkRun, c->capT + 1, 4); ENSURE(cflags, c->capT + 1, 4);
+  ENSURE(connS, (c->capT + 31) / 32 + 1, 4); ENSURE(nonConnS, (c->capT + 31) / 32 + 1, 4);
+  ENSURE(connW, (c->capT + 31) / 32 + 1, 4); ENSURE(nonConnW, (c->capT + 31) / 32 + 1, 4);
   ENSURE(connIdx, c->capT, 4); ENSURE(nonConnIdx, c->capT, 4); ENSURE(pt, c->capT, 4);
   ENSURE(basis, c->capLinks, 4); ENSURE(follower, c->capLinks, 4);
   ENSURE(states, c->capT, 4); ENSURE(inStart, c->capT + 1, 4); ENSURE(inCursor, c->capT, 4);
@@ -904,7 +915,7 @@ void trax_destroy(trax_ctx* c) {
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
                     &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
-                    &c->segStart, &c->linkCount, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS,
+                    &c->segStart, &c->linkCount, &c->linkRun, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS, &c->connW, &c->nonConnW,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,
                     &c->isBest, &c->handlers, &c->tracks, &c->scanScratch, &c->slots, &c->fitOk, &c->fitSegCnt,
                     &c->fitSegDelta, &c->fitRows, &c->fitPartials, &c->fitOut, &c->fitParams, &c->fitDHits,

@@ -88,8 +88,8 @@ __global__ void __launch_bounds__(256)
     conn_kernel(DevConfig cfg, const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
                 const uint32_t* __restrict__ h1, const uint32_t* __restrict__ h2, const uint32_t* __restrict__ h3,
                 const uint32_t* nTDev, const float* __restrict__ eta, const uint32_t* __restrict__ offsets,
-                const uint32_t* __restrict__ segStart, uint32_t* linkCount, uint32_t* flags, uint32_t* basis,
-                uint32_t* follower, uint32_t capLinks, bool sortedSegments) {
+                const uint32_t* __restrict__ segStart, uint32_t* linkCount, uint32_t* flags, uint32_t* runStart,
+                uint32_t* basis, uint32_t* follower, uint32_t capLinks, bool sortedSegments) {
   const uint32_t S = cfg.E * cfg.nLT;
   const uint32_t nT = S > 0 ? *nTDev : 0u;
   const float dEtaCut = cfg.dEtaCut;
@@ -101,6 +101,7 @@ __global__ void __launch_bounds__(256)
       limit = linkCount[t + 1] - pos;
       if (pos >= capLinks) limit = 0;
       else if (limit > capLinks - pos) limit = capLinks - pos;
+      if (limit == 0) continue;  // no links of this basis to write
     }
     bool ok = !(t >= offsets[S - 1]);  // :113-115 (nOffsets - 2 == S - 1)
     uint32_t begin = 0, end = 0, k = 0;
@@ -121,7 +122,17 @@ __global__ void __launch_bounds__(256)
       const float localEta = eta[t];
       // sorted segments: binary search to the (h2, h1) run; otherwise scan
       // the whole range like the reference (caller-provided triplets)
-      for (uint32_t i = sortedSegments ? key_lower_bound(h1, h2, lo, hi, inner, outer) : lo; i < hi; ++i) {
+      // the count pass leaves the run's start for the store pass
+      uint32_t first = lo;
+      if (sortedSegments) {
+        if (EMIT) {
+          first = runStart[t];
+        } else {
+          first = key_lower_bound(h1, h2, lo, hi, inner, outer);
+          runStart[t] = first;
+        }
+      }
+      for (uint32_t i = first; i < hi; ++i) {
         if (h2[i] != outer || h1[i] != inner) {
           if (sortedSegments) break;
           continue;
@@ -148,24 +159,44 @@ __global__ void __launch_bounds__(256)
   if (!EMIT && blockIdx.x == 0 && threadIdx.x == 0) linkCount[nT] = 0u;
 }
 
-// predicate streams over the first nT-1 triplets (Q9), +1 slot zeroed
-__global__ void conn_streams_kernel(const uint32_t* __restrict__ flags, const uint32_t* nTDev, uint32_t* conn,
-                                    uint32_t* nonConn) {
+// The Q9 predicate streams over the first nT-1 triplets as words of 32
+// flags: connectable (flag set) and non-connectable (flag clear), with the
+// number set in each word (+1 slots zeroed; the number of words to
+// *nWordsOut), so that the two compactions scan one value per 32 triplets.
+__global__ void conn_words_kernel(const uint32_t* __restrict__ flags, const uint32_t* nTDev, uint32_t* connWords,
+                                  uint32_t* connSums, uint32_t* nonWords, uint32_t* nonSums, uint32_t* nWordsOut) {
   const uint32_t nT = *nTDev;
-  GRID_STRIDE(k, nT + 1) {
-    const bool inRange = nT > 0 && k < nT - 1;
-    const uint32_t f = inRange ? flags[k] : 0u;
-    conn[k] = inRange ? (f ? 1u : 0u) : 0u;
-    nonConn[k] = inRange ? (f ? 0u : 1u) : 0u;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < nT; base += gridDim.x * blockDim.x) {
+    const uint32_t k = base + lane;
+    const bool inRange = k + 1 < nT;
+    const bool f = inRange && flags[k] != 0u;
+    const uint32_t cw = __ballot_sync(0xffffffffu, f), nw = __ballot_sync(0xffffffffu, inRange && !f);
+    if (lane == 0) {
+      connWords[base >> 5] = cw;
+      connSums[base >> 5] = (uint32_t)__popc(cw);
+      nonWords[base >> 5] = nw;
+      nonSums[base >> 5] = (uint32_t)__popc(nw);
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const uint32_t nW = (nT + 31u) >> 5;
+    connSums[nW] = 0u;
+    nonSums[nW] = 0u;
+    *nWordsOut = nW;
   }
 }
 
-__global__ void compact_kernel(const uint32_t* __restrict__ scan, const uint32_t* nTDev, uint32_t* out,
-                               uint32_t capOut) {
+// out[wordStart[k / 32] + (bits below k in its word)] = k for every set bit
+__global__ void compact_words_kernel(const uint32_t* __restrict__ words, const uint32_t* __restrict__ wordStart,
+                                     const uint32_t* nTDev, uint32_t* out, uint32_t capOut) {
   const uint32_t nT = *nTDev;
   GRID_STRIDE(k, nT) {
-    const uint32_t p = scan[k];
-    if (scan[k + 1] != p && p < capOut) out[p] = k;
+    const uint32_t w = words[k >> 5], bit = k & 31u;
+    if ((w >> bit) & 1u) {
+      const uint32_t p = wordStart[k >> 5] + (uint32_t)__popc(w & ((1u << bit) - 1u));
+      if (p < capOut) out[p] = k;
+    }
   }
 }
 
@@ -319,32 +350,36 @@ cudaError_t segment_bounds(const DevConfig& cfg, const uint32_t* seg, const uint
 
 cudaError_t connectivity_tasks(const DevConfig& cfg, bool emit, DevHits hits, TripletView t, const float* eta,
                                const uint32_t* offsets, const uint32_t* segStart, uint32_t* linkCount,
-                               uint32_t* flags, uint32_t* basis, uint32_t* follower, uint64_t capLinks,
-                               bool sortedSegments, cudaStream_t st, uint32_t* launches) {
+                               uint32_t* flags, uint32_t* runStart, uint32_t* basis, uint32_t* follower,
+                               uint64_t capLinks, bool sortedSegments, cudaStream_t st, uint32_t* launches) {
   const int blocks = grid_for(t.maxN + 1, 256);
   const uint32_t cap = capLinks > 0xffffffffull ? 0xffffffffu : (uint32_t)capLinks;
   if (emit)
     conn_kernel<true><<<blocks, 256, 0, st>>>(cfg, hits.evt, hits.layer, t.h1, t.h2, t.h3, t.nDev, eta, offsets,
-                                              segStart, linkCount, flags, basis, follower, cap, sortedSegments);
+                                              segStart, linkCount, flags, runStart, basis, follower, cap,
+                                              sortedSegments);
   else
     conn_kernel<false><<<blocks, 256, 0, st>>>(cfg, hits.evt, hits.layer, t.h1, t.h2, t.h3, t.nDev, eta, offsets,
-                                               segStart, linkCount, flags, basis, follower, cap, sortedSegments);
+                                               segStart, linkCount, flags, runStart, basis, follower, cap,
+                                               sortedSegments);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }
 
-cudaError_t connectable_streams(const uint32_t* flags, const uint32_t* nTDev, uint64_t maxT, uint32_t* conn,
-                                uint32_t* nonConn, cudaStream_t st, uint32_t* launches) {
-  conn_streams_kernel<<<grid_for(maxT + 1, 256), 256, 0, st>>>(flags, nTDev, conn, nonConn);
+cudaError_t connectable_words(const uint32_t* flags, const uint32_t* nTDev, uint64_t maxT, uint32_t* connWords,
+                              uint32_t* connSums, uint32_t* nonWords, uint32_t* nonSums, uint32_t* nWordsOut,
+                              cudaStream_t st, uint32_t* launches) {
+  conn_words_kernel<<<grid_for(maxT + 1, 256), 256, 0, st>>>(flags, nTDev, connWords, connSums, nonWords, nonSums,
+                                                             nWordsOut);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }
 
-cudaError_t compact_indices(const uint32_t* scan, const uint32_t* nTDev, uint64_t maxT, uint32_t* outIdx,
-                            uint64_t capOut, cudaStream_t st, uint32_t* launches) {
+cudaError_t compact_words(const uint32_t* words, const uint32_t* wordStart, const uint32_t* nTDev, uint64_t maxT,
+                          uint32_t* outIdx, uint64_t capOut, cudaStream_t st, uint32_t* launches) {
   if (maxT == 0) return cudaSuccess;
   const uint32_t cap = capOut > 0xffffffffull ? 0xffffffffu : (uint32_t)capOut;
-  compact_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(scan, nTDev, outIdx, cap);
+  compact_words_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(words, wordStart, nTDev, outIdx, cap);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

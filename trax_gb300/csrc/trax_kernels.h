@@ -118,15 +118,21 @@ cudaError_t triplet_eta(const DevConfig& cfg, DevHits hits, TripletView t, float
                         cudaStream_t st, uint32_t* launches);
 cudaError_t segment_bounds(const DevConfig& cfg, const uint32_t* seg, const uint32_t* nTDev, uint32_t* segStart,
                            cudaStream_t st, uint32_t* launches);
+// runStart[t]: where the count pass found the (h2, h1) run of t's
+// followers in sorted segments; the store pass starts there
 cudaError_t connectivity_tasks(const DevConfig& cfg, bool emit, DevHits hits, TripletView t, const float* eta,
                                const uint32_t* offsets, const uint32_t* segStart, uint32_t* linkCount,
-                               uint32_t* flags, uint32_t* basis, uint32_t* follower, uint64_t capLinks,
-                               bool sortedSegments, cudaStream_t st, uint32_t* launches);
-// flags[k] for k < n-1 -> (flag, !flag) streams for the two compactions; element n-1 and the +1 slot are 0
-cudaError_t connectable_streams(const uint32_t* flags, const uint32_t* nTDev, uint64_t maxT, uint32_t* conn,
-                                uint32_t* nonConn, cudaStream_t st, uint32_t* launches);
-cudaError_t compact_indices(const uint32_t* scan, const uint32_t* nTDev, uint64_t maxT, uint32_t* outIdx,
-                            uint64_t capOut, cudaStream_t st, uint32_t* launches);
+                               uint32_t* flags, uint32_t* runStart, uint32_t* basis, uint32_t* follower,
+                               uint64_t capLinks, bool sortedSegments, cudaStream_t st, uint32_t* launches);
+// flags[k] for k < n-1 -> words of 32 (flag) and (!flag) bits with the number
+// set per word (+1 slots zeroed, the number of words to *nWordsOut)
+cudaError_t connectable_words(const uint32_t* flags, const uint32_t* nTDev, uint64_t maxT, uint32_t* connWords,
+                              uint32_t* connSums, uint32_t* nonWords, uint32_t* nonSums, uint32_t* nWordsOut,
+                              cudaStream_t st, uint32_t* launches);
+// with the sums scanned into wordStart: outIdx[wordStart[k / 32] + (bits
+// below k in its word)] = k for every set bit k < *nTDev
+cudaError_t compact_words(const uint32_t* words, const uint32_t* wordStart, const uint32_t* nTDev, uint64_t maxT,
+                          uint32_t* outIdx, uint64_t capOut, cudaStream_t st, uint32_t* launches);
 // *dst = data[n] (n = *nDev, or nHost when nDev is null): the total a scan of
 // n+1 elements left in its last slot, clamped to cap (TRAX_EBIT_CAPACITY)
 cudaError_t publish_total(const uint32_t* data, const uint32_t* nDev, uint64_t nHost, uint64_t cap, uint32_t* dst,
