@@ -632,9 +632,10 @@ int stage_ca(trax_ctx* c, Mode mode) {
   if (mode == SYNCED) CK(ensure(c, c->scanScratch, scan_scratch_bytes(maxT + 1)));
   CK(scan_exclusive(b.inStart, b.inStart, c->nT + 1, mode == DEVICE ? nTDev : nullptr, 1, maxT + 1,
                     c->scanScratch.p, dev_err(c), c->st, &c->launches, true));
-  CK(ca_fill(ptr<uint32_t>(c->follower), nLinksDev, maxLinks, b, nTDev, maxT, c->st, &c->launches));
-  CK(ca_forward(c->cfg, ptr<uint32_t>(c->basis), b, nTDev, maxT, c->st, &c->launches));
-  CK(ca_backward(ptr<uint32_t>(c->basis), ptr<float>(c->pt), b, nTDev, maxT, nLinksDev, c->st, &c->launches));
+  CK(ca_fill(ptr<uint32_t>(c->basis), ptr<uint32_t>(c->follower), nLinksDev, maxLinks, b, nTDev, maxT, c->st,
+             &c->launches));
+  CK(ca_forward(c->cfg, b, nTDev, maxT, c->st, &c->launches));
+  CK(ca_backward(ptr<float>(c->pt), b, nTDev, maxT, nLinksDev, c->st, &c->launches));
   RC(scan_publish(c, mode, b.handlers, c->nT, mode == DEVICE ? nTDev : nullptr, maxT, S_TRACKS,
                   mode == DEVICE ? c->capTracks : NO_CAP));
   uint64_t maxTracks = c->capTracks;

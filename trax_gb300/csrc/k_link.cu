@@ -223,16 +223,21 @@ __global__ void in_degree_kernel(const uint32_t* __restrict__ follower, const ui
   GRID_STRIDE(p, n) atomicAdd(&inDeg[follower[p]], 1u);
 }
 
-__global__ void in_fill_kernel(const uint32_t* __restrict__ follower, const uint32_t* nLinksDev,
-                               const uint32_t* __restrict__ inStart, uint32_t* cursor, uint32_t* inList) {
+// The bases of each follower's incoming links.  Links are stored in basis
+// order, so the bases of one follower (all distinct) sort like the link
+// indices do.
+__global__ void in_fill_kernel(const uint32_t* __restrict__ basis, const uint32_t* __restrict__ follower,
+                               const uint32_t* nLinksDev, const uint32_t* __restrict__ inStart, uint32_t* cursor,
+                               uint32_t* inList) {
   const uint32_t n = *nLinksDev;
   GRID_STRIDE(p, n) {
     const uint32_t f = follower[p];
-    inList[inStart[f] + atomicAdd(&cursor[f], 1u)] = p;
+    inList[inStart[f] + atomicAdd(&cursor[f], 1u)] = basis[p];
   }
 }
 
-// link indices of each follower in ascending order (insertion sort; lists are short)
+// the incoming bases of each follower in ascending order, which is the
+// order of their links (insertion sort; lists are short)
 __global__ void in_sort_kernel(const uint32_t* __restrict__ inStart, const uint32_t* nTDev, uint32_t* inList) {
   const uint32_t nT = *nTDev;
   GRID_STRIDE(t, nT) {
@@ -249,28 +254,38 @@ __global__ void in_sort_kernel(const uint32_t* __restrict__ inStart, const uint3
   }
 }
 
-__global__ void fill_u32_kernel(uint32_t* p, const uint32_t* nDev, uint32_t add, uint32_t v) {
-  const uint32_t n = *nDev + add;
-  GRID_STRIDE(i, n) p[i] = v;
+// the CA's per-triplet state before a run: in-degrees and cursors 0,
+// states 1, no best basis
+__global__ void ca_init_kernel(CABuffers b, const uint32_t* nTDev) {
+  const uint32_t nT = *nTDev;
+  GRID_STRIDE(i, nT + 1) {
+    b.inStart[i] = 0u;
+    if (i < nT) {
+      b.inCursor[i] = 0u;
+      b.states[i] = 1u;
+      b.best[i] = TRAX_SENTINEL;
+      b.isBest[i] = 0u;
+    }
+  }
 }
 
 // one layer-triplet level of the forward phase
-__global__ void ca_level_kernel(DevConfig cfg, uint32_t level, const uint32_t* __restrict__ basis,
-                                const uint32_t* __restrict__ segOf, const uint32_t* __restrict__ inStart,
-                                const uint32_t* __restrict__ inList, const uint32_t* nTDev, uint32_t* states) {
+__global__ void ca_level_kernel(DevConfig cfg, uint32_t level, const uint32_t* __restrict__ segOf,
+                                const uint32_t* __restrict__ inStart, const uint32_t* __restrict__ inList,
+                                const uint32_t* nTDev, uint32_t* states) {
   const uint32_t nT = *nTDev;
   GRID_STRIDE(t, nT) {
     if (segOf[t] % cfg.nLT != level) continue;
     const uint32_t a = inStart[t], b = inStart[t + 1];
     if (a == b) continue;
     uint32_t m = 0;
-    for (uint32_t j = a; j < b; ++j) m = max(m, states[basis[inList[j]]]);
+    for (uint32_t j = a; j < b; ++j) m = max(m, states[inList[j]]);
     states[t] = m + 1;
   }
 }
 
 // followerBestBasisStore semantics (CellularAutomaton.h:212-263)
-__global__ void ca_best_kernel(const uint32_t* __restrict__ basis, const float* __restrict__ pt,
+__global__ void ca_best_kernel(const float* __restrict__ pt,
                                const uint32_t* __restrict__ inStart, const uint32_t* __restrict__ inList,
                                const uint32_t* __restrict__ states, const uint32_t* nTDev, uint32_t* best,
                                uint32_t* isBest) {
@@ -282,7 +297,7 @@ __global__ void ca_best_kernel(const uint32_t* __restrict__ basis, const float* 
     float minPt = 0.0f;
     uint32_t minIdx = 0;
     for (uint32_t j = a; j < b; ++j) {
-      const uint32_t bb = basis[inList[j]];
+      const uint32_t bb = inList[j];
       if (states[bb] + 1 != sf) continue;
       const float d = fabs_(pt[bb] - pt[t]);
       if (!have) {
@@ -394,7 +409,7 @@ cudaError_t circle_fit(DevHits hits, TripletView t, const uint32_t* connectable,
 
 cudaError_t ca_in_degree(const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks, CABuffers b,
                          const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches) {
-  fill_u32_kernel<<<grid_for(maxT + 1, 256), 256, 0, st>>>(b.inStart, nTDev, 1, 0u);
+  ca_init_kernel<<<grid_for(maxT + 1, 256), 256, 0, st>>>(b, nTDev);
   if (launches) *launches += 1;
   if (maxLinks > 0) {
     in_degree_kernel<<<grid_for(maxLinks, 256), 256, 0, st>>>(follower, nLinksDev, b.inStart);
@@ -403,12 +418,11 @@ cudaError_t ca_in_degree(const uint32_t* follower, const uint32_t* nLinksDev, ui
   return cudaGetLastError();
 }
 
-cudaError_t ca_fill(const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks, CABuffers b,
-                    const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches) {
-  fill_u32_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(b.inCursor, nTDev, 0, 0u);
-  if (launches) *launches += 1;
+cudaError_t ca_fill(const uint32_t* basis, const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks,
+                    CABuffers b, const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches) {
   if (maxLinks > 0) {
-    in_fill_kernel<<<grid_for(maxLinks, 256), 256, 0, st>>>(follower, nLinksDev, b.inStart, b.inCursor, b.inList);
+    in_fill_kernel<<<grid_for(maxLinks, 256), 256, 0, st>>>(basis, follower, nLinksDev, b.inStart, b.inCursor,
+                                                            b.inList);
     if (launches) *launches += 1;
   }
   in_sort_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(b.inStart, nTDev, b.inList);
@@ -416,26 +430,20 @@ cudaError_t ca_fill(const uint32_t* follower, const uint32_t* nLinksDev, uint64_
   return cudaGetLastError();
 }
 
-cudaError_t ca_forward(const DevConfig& cfg, const uint32_t* basis, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
-                       cudaStream_t st, uint32_t* launches) {
-  fill_u32_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(b.states, nTDev, 0, 1u);
-  if (launches) *launches += 1;
+cudaError_t ca_forward(const DevConfig& cfg, CABuffers b, const uint32_t* nTDev, uint64_t maxT, cudaStream_t st,
+                       uint32_t* launches) {
   for (uint32_t level = 1; level < cfg.nLT; ++level) {
-    ca_level_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(cfg, level, basis, b.segOf, b.inStart, b.inList, nTDev,
-                                                         b.states);
+    ca_level_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(cfg, level, b.segOf, b.inStart, b.inList, nTDev, b.states);
     if (launches) *launches += 1;
   }
   return cudaGetLastError();
 }
 
-cudaError_t ca_backward(const uint32_t* basis, const float* pt, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
+cudaError_t ca_backward(const float* pt, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
                         const uint32_t* nLinksDev, cudaStream_t st, uint32_t* launches) {
-  fill_u32_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(b.best, nTDev, 0, TRAX_SENTINEL);
-  fill_u32_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(b.isBest, nTDev, 0, 0u);
-  ca_best_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(basis, pt, b.inStart, b.inList, b.states, nTDev, b.best,
-                                                      b.isBest);
+  ca_best_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(pt, b.inStart, b.inList, b.states, nTDev, b.best, b.isBest);
   handlers_kernel<<<grid_for(maxT + 1, 256), 256, 0, st>>>(b.states, b.isBest, nTDev, nLinksDev, b.handlers);
-  if (launches) *launches += 4;
+  if (launches) *launches += 2;
   return cudaGetLastError();
 }
 

@@ -146,7 +146,7 @@ struct CABuffers {
   uint32_t* states;    // [nT]
   uint32_t* inStart;   // [nT+1]
   uint32_t* inCursor;  // [nT]
-  uint32_t* inList;    // [nLinks] link indices grouped by follower
+  uint32_t* inList;    // [nLinks] bases of the incoming links, grouped by follower
   uint32_t* best;      // [nT]
   uint32_t* isBest;    // [nT]
   uint32_t* handlers;  // [nT+1]
@@ -155,11 +155,11 @@ struct CABuffers {
 
 cudaError_t ca_in_degree(const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks, CABuffers b,
                          const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches);
-cudaError_t ca_fill(const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks, CABuffers b,
-                    const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches);
-cudaError_t ca_forward(const DevConfig& cfg, const uint32_t* basis, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
-                       cudaStream_t st, uint32_t* launches);
-cudaError_t ca_backward(const uint32_t* basis, const float* pt, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
+cudaError_t ca_fill(const uint32_t* basis, const uint32_t* follower, const uint32_t* nLinksDev, uint64_t maxLinks,
+                    CABuffers b, const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches);
+cudaError_t ca_forward(const DevConfig& cfg, CABuffers b, const uint32_t* nTDev, uint64_t maxT, cudaStream_t st,
+                       uint32_t* launches);
+cudaError_t ca_backward(const float* pt, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
                         const uint32_t* nLinksDev, cudaStream_t st, uint32_t* launches);
 cudaError_t ca_tracks(CABuffers b, const uint32_t* nTDev, uint64_t maxT, uint32_t* tracks, uint64_t maxTracks,
                       uint32_t* err, cudaStream_t st, uint32_t* launches);
