@@ -176,7 +176,7 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells):
 # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # same chain on the first 300 events of the workload; a full launch scales
 # them by its units (traffic grows with pairs, candidates and hits).
-TRAFFIC_PER_UNIT = {"predict_count": ("pairs", 32.3), "filter": ("candidates", 25.7), "grid_build": ("hits", 111.0)}
+TRAFFIC_PER_UNIT = {"predict_count": ("pairs", 32.3), "filter": ("candidates", 26.1), "grid_build": ("hits", 96.7)}
 
 
 def kernel_traffic(name, st, n_hits):
