@@ -179,6 +179,33 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells):
 TRAFFIC_PER_UNIT = {"predict_count": ("pairs", 32.3), "filter": ("candidates", 26.1), "grid_build": ("hits", 96.7)}
 
 
+# warp instructions per unit of work (ncu smsp__inst_executed.sum of the same
+# 300-event capture / its units): the dominant kernels are issue-bound, so
+# their position against the SMs' issue rate is reported beside the HBM one
+INST_PER_UNIT = {"predict_count": ("pairs", 31.41)}
+
+
+def kernel_issue(name, st, ms, clk, device):
+    """Issue roofline of a kernel: warp instructions per second against one
+    instruction per cycle on each of the SMs' four schedulers at the SM clock
+    seen during the timed region."""
+    import torch
+    if name not in INST_PER_UNIT or not ms:
+        return None
+    unit, per = INST_PER_UNIT[name]
+    n = {"pairs": st.n_pairs}[unit]
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    if not mhz:
+        return None
+    achieved = per * n / (ms * 1e-3)
+    peak = sms * 4 * mhz * 1e6
+    return {"achieved": round(achieved / 1e9, 1), "peak": round(peak / 1e9, 1), "unit": "G warp inst/s",
+            "frac": round(achieved / peak, 4),
+            "note": f"{per} warp instructions per {unit[:-1]} (ncu, 300-event case) x units / live kernel time; "
+                    f"peak = {sms} SMs x 4 schedulers x {mhz:.0f} MHz"}
+
+
 def kernel_traffic(name, st, n_hits):
     if name not in TRAFFIC_PER_UNIT:
         return None
@@ -364,6 +391,7 @@ def run_ours(args, ranks):
                      "traffic_note": "DRAM bytes per launch: ncu per-unit traffic of the 300-event case x units",
                      "peak_kind": f"{peak_kind} hbm_gbs (copy bandwidth)",
                      "algorithmic_bytes": int(kb)},
+        "issue_roofline": kernel_issue(dom, st, kmean[dom], clk, device),
         "chain_roofline": {"achieved": round(cb / (ms_per_step * 1e-3) / 1e9, 2), "unit": "GB/s",
                            "frac": round(cb / (ms_per_step * 1e-3) / 1e9 / hbm, 4), "bytes_per_step": int(cb)},
         "gpu_launches": int(launches),
