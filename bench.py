@@ -392,6 +392,12 @@ def run_ours(args, ranks):
                      "peak_kind": f"{peak_kind} hbm_gbs (copy bandwidth)",
                      "algorithmic_bytes": int(kb)},
         "issue_roofline": kernel_issue(dom, st, kmean[dom], clk, device),
+        # window and cut evaluations per second of the FP32-heavy kernels:
+        # one pair window per outer hit, one third-hit window per pair, the
+        # dphi test per candidate (the rest on its survivors)
+        "tests_per_s": {k: round(n / (kmean[kk] * 1e-3), 1) for k, kk, n in (
+            ("pair_windows", "pair_count", n_tasks), ("predict_windows", "predict_count", st.n_pairs),
+            ("filter_candidates", "filter", st.n_candidates)) if kmean.get(kk)},
         "chain_roofline": {"achieved": round(cb / (ms_per_step * 1e-3) / 1e9, 2), "unit": "GB/s",
                            "frac": round(cb / (ms_per_step * 1e-3) / 1e9 / hbm, 4), "bytes_per_step": int(cb)},
         "gpu_launches": int(launches),
