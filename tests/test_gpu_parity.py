@@ -285,6 +285,32 @@ def test_grid_build_hit_arrays_outside_shared_memory(ctx, oracle_lib):
     compare(ctx.results(), ref)
 
 
+def test_layer_beyond_16bit_grid_counters(ctx, oracle_lib):
+    """The grid build counts in 16-bit halves while every layer has fewer
+    than 65 536 hits; a layer of 71 216 hits (on layer 10, which no layer
+    triplet uses) takes the 32-bit build with its per-hit arrays in global
+    scratch, in the synced path and in a captured graph."""
+    b = events.generate(2, n_events=2, seed=4)
+    rng = np.random.default_rng(9)
+    n_add = 70000
+    phi = rng.uniform(-np.pi, np.pi, n_add)
+    new = {"x": (78.0 * np.cos(phi)).astype(np.float32), "y": (78.0 * np.sin(phi)).astype(np.float32),
+           "z": rng.uniform(-100, 100, n_add).astype(np.float32), "layer": np.full(n_add, 10, np.uint32),
+           "det_id": np.zeros(n_add, np.uint32), "hit_id": np.arange(n_add, dtype=np.uint32) + 10 ** 6,
+           "event": np.zeros(n_add, np.uint32)}
+    end0 = int(b.event_offsets[1])  # event 0 ends with its layer-10 hits
+    cols = {k: np.concatenate([getattr(b, k)[:end0], new[k].astype(getattr(b, k).dtype), getattr(b, k)[end0:]])
+            for k in new}
+    lh = b.layer_hits.copy()
+    lh[0, 9] += n_add
+    big = events._assemble(cols, lh, b)
+    assert big.layer_hits.max() > 0xffff
+    ref = oracle_lib.run(big)[0]
+    compare(stagewise(ctx, big), ref)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
 def test_capacity_overflow_recalibrates(ctx, oracle_lib):
     """A batch of the same shape but far denser hits overflows the capacities
     calibrated on the first: the call recalibrates, recaptures and returns the

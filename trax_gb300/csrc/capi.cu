@@ -751,6 +751,7 @@ uint64_t shape_key(trax_ctx* c, bool linking) {
     k *= 1099511628211ull;
   };
   mix(c->E); mix(c->L); mix(c->nHits); mix(c->cfg.C); mix(c->cfg.nLT); mix(linking ? 1 : 0);
+  mix(c->maxLayerHits > 0xffffu ? 1 : 0);  // the grid build's 16-bit counters hold layers below 65 536 hits
   mix(c->bufGeneration); mix(c->capTasks); mix(c->capPairs); mix(c->capCands); mix(c->capT); mix(c->capLinks);
   mix(c->capTracks);
   const unsigned char* b = reinterpret_cast<const unsigned char*>(&c->cfg);

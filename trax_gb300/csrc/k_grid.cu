@@ -138,6 +138,177 @@ __global__ void __launch_bounds__(GRID_THREADS)
   }
 }
 
+// The same for layers of fewer than 65 536 hits and grids of fewer than
+// 65 536 cells, in about half the shared memory, so that more CTAs share an
+// SM: the cell counters are 16-bit halves of 32-bit words (two cells per
+// word; a counter never passes the layer's hit count, so a half never
+// carries into the other), and each hit's cell and slot are 16-bit.  The
+// layout: phi [maxHits] f32, counters [(C + 1) / 2] u32, cell [maxHits] u16,
+// slot [maxHits] u16.  A layer with more than maxHits hits keeps its per-hit
+// arrays in global scratch.
+__device__ __forceinline__ uint32_t half_of(uint32_t word, uint32_t c) { return (word >> ((c & 1u) * 16u)) & 0xffffu; }
+
+__global__ void __launch_bounds__(GRID_THREADS)
+    grid_kernel16(DevConfig cfg, GridInput in, uint32_t* __restrict__ grid, DevHits out, GridScratch sc,
+                  uint32_t* err, uint32_t maxHits) {
+  extern __shared__ uint32_t smem[];
+  __shared__ uint32_t s_warpSum[GRID_WARPS];
+  const uint32_t task = blockIdx.x;  // event * L + layer
+  const uint32_t e = task / cfg.L;
+  const uint32_t C = cfg.C, W = (C + 1) / 2;
+  const uint32_t n = in.layerHits[task];
+  const uint32_t base = in.eventOffsets[e] + in.layerOffsets[task];
+  float* phiS = reinterpret_cast<float*>(smem);
+  uint32_t* cnt = smem + maxHits;  // two 16-bit counters per word
+  uint16_t* cellS = reinterpret_cast<uint16_t*>(cnt + W);
+  uint16_t* permS = cellS + maxHits;
+  const bool inSmem = n <= maxHits;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  if (n > 0xffffu) {
+    // 16-bit counters cannot hold this layer (the launch is chosen for
+    // layers below 65 536 hits): flag it and leave a consistent layer --
+    // no cell holds a hit, the hits in input order
+    if (tid == 0) raise_error(err, TRAX_EBIT_BOUNDS);
+    uint32_t* gl = grid + (size_t)task * C;
+    for (uint32_t c = tid; c < C; c += GRID_THREADS) gl[c] = base;
+    for (uint32_t s = tid; s < n; s += GRID_THREADS) {
+      const uint32_t k = base + s;
+      const float x = in.x[k], y = in.y[k], z = in.z[k];
+      out.x[k] = x;
+      out.y[k] = y;
+      out.z[k] = z;
+      out.layer[k] = in.layer[k];
+      out.det[k] = in.det[k];
+      out.hid[k] = in.hid[k];
+      out.evt[k] = in.evt[k];
+      out.orig[k] = k;
+      out.xyzp[k] = make_float4(x, y, z, 0.0f);
+    }
+    return;
+  }
+
+  for (uint32_t w = tid; w < W; w += GRID_THREADS) cnt[w] = 0u;
+  __syncthreads();
+
+  // 1. cells (gridCount, GridBuilder.h:80-87)
+  for (uint32_t i = tid; i < n; i += GRID_THREADS) {
+    const uint32_t k = base + i;
+    const float x = in.x[k], y = in.y[k], z = in.z[k];
+    uint32_t zSector = f2u_sat(floor_(div_(z - cfg.minZ, cfg.sZ)));
+    float phi = atan2_(y, x);
+    uint32_t phiSector = f2u_sat(floor_(div_(phi - cfg.minPhi, cfg.sP)));
+    if (zSector >= cfg.nZ || phiSector > cfg.nP) {
+      raise_error(err, TRAX_EBIT_BOUNDS);
+      zSector = min(zSector, cfg.nZ - 1);
+      phiSector = min(phiSector, cfg.nP);
+    }
+    const uint32_t cell = zSector * (cfg.nP + 1) + phiSector;
+    if (inSmem) {
+      cellS[i] = (uint16_t)cell;
+      phiS[i] = phi;
+    } else {
+      sc.cell[k] = cell;
+      sc.phi[k] = phi;
+    }
+    atomicAdd(&cnt[cell >> 1], 1u << ((cell & 1u) * 16u));
+  }
+  __syncthreads();
+
+  // 2. CTA exclusive scan of the counters over whole words per thread;
+  //    write the grid boundaries
+  const uint32_t chunkW = (W + GRID_THREADS - 1) / GRID_THREADS;
+  const uint32_t w0 = min(tid * chunkW, W), w1 = min(w0 + chunkW, W);
+  uint32_t local = 0;
+  for (uint32_t w = w0; w < w1; ++w) {
+    const uint32_t v = cnt[w];
+    local += (v & 0xffffu) + (v >> 16);
+  }
+  uint32_t incl = local;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += t;
+  }
+  if (lane == 31) s_warpSum[warp] = incl;
+  __syncthreads();
+  uint32_t warpOff = 0;
+  for (uint32_t w = 0; w < warp; ++w) warpOff += s_warpSum[w];
+  uint32_t run = warpOff + incl - local;
+  __syncthreads();
+  for (uint32_t w = w0; w < w1; ++w) {
+    const uint32_t v = cnt[w];
+    const uint32_t lo = run, hi = run + (v & 0xffffu);  // the next free slots of cells 2w and 2w + 1
+    cnt[w] = lo | (hi << 16);
+    run = hi + (v >> 16);
+  }
+  __syncthreads();
+  // the boundaries, written with consecutive threads on consecutive cells
+  uint32_t* gl = grid + (size_t)task * C;
+  for (uint32_t c = tid; c < C; c += GRID_THREADS) gl[c] = base + half_of(cnt[c >> 1], c);
+  __syncthreads();
+
+  // 3. placement by the cell cursors, then the stable order inside each cell
+  //    (as in grid_kernel); afterwards cursor c is the end of cell c
+  if (inSmem) {
+    for (uint32_t i = tid; i < n; i += GRID_THREADS) {
+      const uint32_t cell = cellS[i];
+      const uint32_t sh = (cell & 1u) * 16u;
+      permS[(atomicAdd(&cnt[cell >> 1], 1u << sh) >> sh) & 0xffffu] = (uint16_t)i;
+    }
+  } else {
+    for (uint32_t i = tid; i < n; i += GRID_THREADS) {
+      const uint32_t cell = sc.cell[base + i];
+      const uint32_t sh = (cell & 1u) * 16u;
+      sc.perm[base + ((atomicAdd(&cnt[cell >> 1], 1u << sh) >> sh) & 0xffffu)] = i;
+    }
+  }
+  __syncthreads();
+  for (uint32_t c = tid; c < C; c += GRID_THREADS) {
+    const uint32_t lo = c ? half_of(cnt[(c - 1) >> 1], c - 1) : 0u, hi = half_of(cnt[c >> 1], c);
+    if (hi - lo < 2) continue;
+    if (inSmem) {
+      for (uint32_t a = lo + 1; a < hi; ++a) {  // insertion sort: cells hold a few hits
+        const uint16_t v = permS[a];
+        uint32_t b = a;
+        while (b > lo && permS[b - 1] > v) {
+          permS[b] = permS[b - 1];
+          --b;
+        }
+        permS[b] = v;
+      }
+    } else {
+      uint32_t* p = sc.perm + base;
+      for (uint32_t a = lo + 1; a < hi; ++a) {
+        const uint32_t v = p[a];
+        uint32_t b = a;
+        while (b > lo && p[b - 1] > v) {
+          p[b] = p[b - 1];
+          --b;
+        }
+        p[b] = v;
+      }
+    }
+  }
+  __syncthreads();
+
+  // 4. gather into cell order (gridStore, GridBuilder.h:243-253)
+  for (uint32_t s = tid; s < n; s += GRID_THREADS) {
+    const uint32_t dst = base + s;
+    const uint32_t i = inSmem ? (uint32_t)permS[s] : sc.perm[dst];
+    const uint32_t src = base + i;
+    const float x = in.x[src], y = in.y[src], z = in.z[src];
+    out.x[dst] = x;
+    out.y[dst] = y;
+    out.z[dst] = z;
+    out.layer[dst] = in.layer[src];
+    out.det[dst] = in.det[src];
+    out.hid[dst] = in.hid[src];
+    out.evt[dst] = in.evt[src];
+    out.orig[dst] = src;
+    out.xyzp[dst] = make_float4(x, y, z, inSmem ? phiS[i] : sc.phi[src]);
+  }
+}
+
 // The uploaded hits taken as the hit collection as they are (identity
 // order), for the linking stages run on caller-provided triplets.
 __global__ void identity_hits_kernel(GridInput in, uint32_t n, DevHits out) {
@@ -165,7 +336,9 @@ cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStre
 }
 
 cudaError_t grid_prepare(int) {
-  return cudaFuncSetAttribute(grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
+  cudaError_t e = cudaFuncSetAttribute(grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(grid_kernel16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
 }
 
 cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid, DevHits out, GridScratch sc,
@@ -175,6 +348,13 @@ cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid
   const int useSmem = cfg.C <= GRID_SMEM_CELLS ? 1 : 0;
   const size_t counterBytes = useSmem ? (size_t)cfg.C * sizeof(uint32_t) : 0;
   const size_t hitBytes = (size_t)maxLayerHits * 3 * sizeof(uint32_t);
+  // 16-bit counters, cells and slots when every index fits
+  const size_t bytes16 = (size_t)maxLayerHits * 8 + (size_t)(cfg.C + 1) / 2 * 4;
+  if (useSmem && cfg.C < 65536u && maxLayerHits < 65536u && bytes16 <= GRID_SMEM_MAX) {
+    grid_kernel16<<<tasks, GRID_THREADS, bytes16, st>>>(cfg, in, grid, out, sc, err, maxLayerHits);
+    if (launches) *launches += 1;
+    return cudaGetLastError();
+  }
   const bool hitsFit = useSmem && counterBytes + hitBytes <= GRID_SMEM_MAX;
   grid_kernel<<<tasks, GRID_THREADS, counterBytes + (hitsFit ? hitBytes : 0), st>>>(
       cfg, in, grid, out, sc, err, useSmem, hitsFit ? maxLayerHits : 0u);
