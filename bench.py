@@ -176,23 +176,27 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells):
 # from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the
 # same chain on the first 300 events of the workload; a full launch scales
 # them by its units (traffic grows with pairs, candidates and hits).
-TRAFFIC_PER_UNIT = {"predict_count": ("pairs", 32.3), "filter": ("candidates", 26.1), "grid_build": ("hits", 96.7)}
+TRAFFIC_PER_UNIT = {  # by grid (nZ x nPhi): the grid changes the cells read and the hits visited
+    "150x64": {"predict_count": ("pairs", 32.5), "filter": ("candidates", 27.3), "grid_build": ("hits", 97.0)},
+    "200x64": {"predict_count": ("pairs", 32.7), "filter": ("candidates", 27.3), "grid_build": ("hits", 110.9)},
+}
 
 
 # warp instructions per unit of work (ncu smsp__inst_executed.sum of the same
 # 300-event capture / its units): the dominant kernels are issue-bound, so
 # their position against the SMs' issue rate is reported beside the HBM one
-INST_PER_UNIT = {"predict_count": ("pairs", 31.41)}
+INST_PER_UNIT = {"150x64": {"predict_count": ("pairs", 30.37)}, "200x64": {"predict_count": ("pairs", 28.76)}}
 
 
-def kernel_issue(name, st, ms, clk, device):
+def kernel_issue(name, st, ms, clk, device, grid):
     """Issue roofline of a kernel: warp instructions per second against one
     instruction per cycle on each of the SMs' four schedulers at the SM clock
     seen during the timed region."""
     import torch
-    if name not in INST_PER_UNIT or not ms:
+    table = INST_PER_UNIT.get(grid, {})
+    if name not in table or not ms:
         return None
-    unit, per = INST_PER_UNIT[name]
+    unit, per = table[name]
     n = {"pairs": st.n_pairs}[unit]
     sms = torch.cuda.get_device_properties(device).multi_processor_count
     mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
@@ -202,14 +206,16 @@ def kernel_issue(name, st, ms, clk, device):
     peak = sms * 4 * mhz * 1e6
     return {"achieved": round(achieved / 1e9, 1), "peak": round(peak / 1e9, 1), "unit": "G warp inst/s",
             "frac": round(achieved / peak, 4),
-            "note": f"{per} warp instructions per {unit[:-1]} (ncu, 300-event case) x units / live kernel time; "
+            "note": f"{per} warp instructions per {unit[:-1]} (ncu, 300-event case, grid {grid}) x units / live "
+                    f"kernel time; "
                     f"peak = {sms} SMs x 4 schedulers x {mhz:.0f} MHz"}
 
 
-def kernel_traffic(name, st, n_hits):
-    if name not in TRAFFIC_PER_UNIT:
+def kernel_traffic(name, st, n_hits, grid):
+    table = TRAFFIC_PER_UNIT.get(grid, {})
+    if name not in table:
         return None
-    unit, per = TRAFFIC_PER_UNIT[name]
+    unit, per = table[name]
     n = {"pairs": st.n_pairs, "candidates": st.n_candidates, "hits": n_hits}[unit]
     return int(per * n)
 
@@ -387,11 +393,12 @@ def run_ours(args, ranks):
         "stage_ms": {k: round(float(np.mean(v)), 4) for k, v in stage.items() if v and min(v) >= 0},
         "kernel_ms": {k: round(v, 4) for k, v in kmean.items()},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 2), "peak": hbm, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": kernel_traffic(dom, st, n_hits),
-                     "traffic_note": "DRAM bytes per launch: ncu per-unit traffic of the 300-event case x units",
+                     "frac": round(achieved / hbm, 4), "traffic": kernel_traffic(dom, st, n_hits, f"{batch.n_z}x{batch.n_phi}"),
+                     "traffic_note": "DRAM bytes per launch: ncu per-unit traffic of the 300-event case at this grid x "
+                                     "units (null for a grid without a capture)",
                      "peak_kind": f"{peak_kind} hbm_gbs (copy bandwidth)",
                      "algorithmic_bytes": int(kb)},
-        "issue_roofline": kernel_issue(dom, st, kmean[dom], clk, device),
+        "issue_roofline": kernel_issue(dom, st, kmean[dom], clk, device, f"{batch.n_z}x{batch.n_phi}"),
         # window and cut evaluations per second of the FP32-heavy kernels:
         # one pair window per outer hit, one third-hit window per pair, the
         # dphi test per candidate (the rest on its survivors)
