@@ -332,6 +332,20 @@ int trax_events_load(const trax_event_set* events, uint64_t first, uint64_t coun
                      uint32_t* event_offsets, uint32_t* layer_hits, uint32_t* layer_offsets, uint32_t* findable_id,
                      uint32_t* findable_event);
 
+/* The same loader with its layer bucketing on the device, straight into the
+ * context (in place of trax_events_load + trax_upload_hits): the host
+ * classifies every hit of events [first, first + count) as addEvent does
+ * (track pT, findability, the track limit) and gives each kept hit its
+ * (layer, push position) key; one CTA per event then sorts the keys and
+ * gathers the hit columns into the context's input arrays.  The context
+ * ends up exactly as after trax_upload_hits with trax_events_load's output.
+ * sizes as trax_events_load; the first min(n_findable, findable_cap)
+ * findable track ids and events are copied out (either may be NULL). */
+int trax_events_upload(trax_ctx* ctx, const trax_event_set* events, uint64_t first, uint64_t count,
+                       const trax_layer_triplet* lt, int n_lt, float min_pt, int num_tracks, int only_tracks,
+                       trax_loaded_sizes* sizes, uint32_t* findable_id, uint32_t* findable_event,
+                       uint64_t findable_cap);
+
 /* GeometrySupplement from the reference's detector tables
  * (TripletBuilder.cpp:140-184): radius_dictionary rows "entry,radius",
  * detector_radius rows "detId,entry,layer"; min/max radius of layers

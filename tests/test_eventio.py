@@ -65,12 +65,12 @@ def encode(events_):
     return out
 
 
-def synthetic_events(seed=3, n_events=4):
+def synthetic_events(seed=3, n_events=4, n_tracks=29):
     rng = np.random.default_rng(seed)
     evs = []
     for e in range(n_events):
         hits = []
-        for t in range(1, 30):
+        for t in range(1, n_tracks + 1):
             pt = float(rng.uniform(0.3, 5.0))
             layers = [l for l in range(1, 10) if rng.uniform() < 0.9]
             for l in layers:
@@ -290,3 +290,49 @@ def test_loaded_events_on_the_gpu_match_the_oracle(eventio, oracle_lib, tmp_path
     b = physics.triplet_records(ref["trip_h1"], ref["trip_h2"], ref["trip_h3"], ref["trip_offsets"],
                                 batch.n_events, len(lts), hid, fid, fev)
     assert a == b
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("num_tracks,only_tracks", [(-1, False), (-1, True), (5, False)])
+def test_device_bucketing_matches_host_loader(eventio, tmp_path, num_tracks, only_tracks):
+    """trax_events_upload (the layer bucketing on the device) leaves a context
+    as trax_events_load + trax_upload_hits do: the same chain results
+    element by element and the same findable tracks.  The last event has more
+    than 4 096 hits, so its keys sort in global scratch."""
+    from trax_gb300 import capi
+    p = tmp_path / "events.pb"
+    evs = synthetic_events(seed=11, n_events=5) + synthetic_events(seed=12, n_events=1, n_tracks=700)
+    for ev in evs:  # radii per layer, as in the test above
+        for h in ev["hits"]:
+            r = 4.0 + 3.0 * h["layer"]
+            n = np.hypot(h["x"], h["y"]) or 1.0
+            h["x"], h["y"], h["z"] = h["x"] / n * r, h["y"] / n * r, h["z"] * 5.0
+    p.write_bytes(encode(evs))
+    f = eventio.EventFile(str(p))
+    assert f.raw(5)["layer"].size > 4096
+    lts = events.layer_triplets([1, 2])
+    batch, fid, fev = f.load(lts, 1.0, num_tracks=num_tracks, only_tracks=only_tracks, n_z=20, n_phi=32)
+    a, b = capi.Context(0), capi.Context(0)
+    try:
+        a.upload(batch)
+        a.seed_batch(use_graph=True)
+        ra = a.results()
+        b.set_layer_triplets(batch.lts, batch.min_pt)
+        b.set_geometry(batch.min_r, batch.max_r)
+        b.set_grid(batch.n_z, batch.n_phi)
+        sizes, fid2, fev2 = f.upload(b, lts, 1.0, num_tracks=num_tracks, only_tracks=only_tracks)
+        b.seed_batch(use_graph=True)
+        rb = b.results()
+    finally:
+        a.close()
+        b.close()
+    assert (sizes["n_hits"], sizes["n_events"]) == (batch.n_hits, batch.n_events)
+    assert np.array_equal(fid, fid2) and np.array_equal(fev, fev2)
+    assert ra["pairs"].size > 0
+    if num_tracks < 0:
+        assert ra["trip_h1"].size > 0
+    for k in ra:
+        x, y = np.asarray(ra[k]), np.asarray(rb[k])
+        if x.dtype == np.float32:
+            x, y = x.view(np.uint32), y.view(np.uint32)
+        assert np.array_equal(x, y), k

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "trax/trax.h"
+#include "trax_events.h"
 #include "trax_kernels.h"
 
 using namespace trax;
@@ -111,6 +112,8 @@ struct trax_ctx {
   DevConfig cfg;
   // inputs
   DevBuf in_x, in_y, in_z, in_layer, in_det, in_hid, in_evt, evOff, layHits, layOff;
+  // event-file hits for the device bucketing (trax_events_upload)
+  DevBuf raw_x, raw_y, raw_z, raw_layer, raw_det, raw_tid, raw_key, raw_off, raw_scratchOff, raw_scratch;
   // grid stage
   DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
   // pair stage
@@ -913,7 +916,8 @@ void trax_destroy(trax_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   drop_graph(c);
   DevBuf* bufs[] = {&c->in_x, &c->in_y, &c->in_z, &c->in_layer, &c->in_det, &c->in_hid, &c->in_evt, &c->evOff,
-                    &c->layHits, &c->layOff, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
+                    &c->layHits, &c->layOff, &c->raw_x, &c->raw_y, &c->raw_z, &c->raw_layer, &c->raw_det,
+                    &c->raw_tid, &c->raw_key, &c->raw_off, &c->raw_scratchOff, &c->raw_scratch, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
                     &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
@@ -1050,6 +1054,70 @@ int trax_upload_hits(trax_ctx* c, const trax_hits_soa* h, uint32_t n_hits, const
   c->maxLayerHits = maxLayer;
   c->haveHits = true;
   c->stage = 0;
+  return TRAX_OK;
+}
+
+int trax_events_upload(trax_ctx* c, const trax_event_set* events, uint64_t first, uint64_t count,
+                       const trax_layer_triplet* lt, int n_lt, float min_pt, int num_tracks, int only_tracks,
+                       trax_loaded_sizes* sizes, uint32_t* findable_id, uint32_t* findable_event,
+                       uint64_t findable_cap) {
+  if (!c || !events || !lt || !sizes) return fail(c, TRAX_ERR_ARG, "null argument");
+  trax::RawEvents raw;
+  if (trax::classify_events(events, first, count, lt, n_lt, min_pt, num_tracks, only_tracks, raw) != TRAX_OK)
+    return fail(c, TRAX_ERR_ARG, "invalid event range, layer triplets or event size");
+  const uint32_t E = (uint32_t)(raw.rawOffsets.size() - 1), L = raw.nLayers;
+  if (L == 0 || L > TRAX_MAX_LAYERS) return fail(c, TRAX_ERR_ARG, "invalid number of layers");
+  const Mode mode = SYNCED;
+  const size_t nRaw = raw.x.size(), n = raw.nHits;
+  // per event: the global sort scratch of events too large for shared memory
+  std::vector<uint32_t> scratchOff(E + 1, 0);
+  for (uint32_t e = 0; e < E; ++e)
+    scratchOff[e + 1] = scratchOff[e] + bucket_scratch_keys(raw.rawOffsets[e + 1] - raw.rawOffsets[e]);
+  ENSURE(raw_x, nRaw, 4); ENSURE(raw_y, nRaw, 4); ENSURE(raw_z, nRaw, 4);
+  ENSURE(raw_layer, nRaw, 4); ENSURE(raw_det, nRaw, 4); ENSURE(raw_tid, nRaw, 4); ENSURE(raw_key, nRaw, 8);
+  ENSURE(raw_off, E + 1, 4); ENSURE(raw_scratchOff, E + 1, 4); ENSURE(raw_scratch, scratchOff[E], 8);
+  ENSURE(in_x, n, 4); ENSURE(in_y, n, 4); ENSURE(in_z, n, 4);
+  ENSURE(in_layer, n, 4); ENSURE(in_det, n, 4); ENSURE(in_hid, n, 4); ENSURE(in_evt, n, 4);
+  ENSURE(evOff, E, 4);
+  ENSURE(layHits, (size_t)E * L, 4);
+  ENSURE(layOff, (size_t)E * L, 4);
+  auto up = [&](DevBuf& d, const void* h, size_t bytes) {
+    return bytes ? cudaMemcpyAsync(d.p, h, bytes, cudaMemcpyHostToDevice, c->st) : cudaSuccess;
+  };
+  CK(up(c->raw_x, raw.x.data(), nRaw * 4));
+  CK(up(c->raw_y, raw.y.data(), nRaw * 4));
+  CK(up(c->raw_z, raw.z.data(), nRaw * 4));
+  CK(up(c->raw_layer, raw.layer.data(), nRaw * 4));
+  CK(up(c->raw_det, raw.det.data(), nRaw * 4));
+  CK(up(c->raw_tid, raw.tid.data(), nRaw * 4));
+  CK(up(c->raw_key, raw.key.data(), nRaw * 8));
+  CK(up(c->raw_off, raw.rawOffsets.data(), (size_t)(E + 1) * 4));
+  CK(up(c->raw_scratchOff, scratchOff.data(), (size_t)(E + 1) * 4));
+  CK(up(c->evOff, raw.eventOffsets.data(), (size_t)E * 4));
+  CK(up(c->layHits, raw.layerHits.data(), (size_t)E * L * 4));
+  CK(up(c->layOff, raw.layerOffsets.data(), (size_t)E * L * 4));
+  RawEventHits in{ptr<float>(c->raw_x), ptr<float>(c->raw_y), ptr<float>(c->raw_z), ptr<uint32_t>(c->raw_layer),
+                  ptr<uint32_t>(c->raw_det), ptr<uint32_t>(c->raw_tid),
+                  ptr<unsigned long long>(c->raw_key), ptr<uint32_t>(c->raw_off),
+                  ptr<uint32_t>(c->raw_scratchOff)};
+  HitColumns out{ptr<float>(c->in_x), ptr<float>(c->in_y), ptr<float>(c->in_z), ptr<uint32_t>(c->in_layer),
+                 ptr<uint32_t>(c->in_det), ptr<uint32_t>(c->in_hid), ptr<uint32_t>(c->in_evt),
+                 ptr<uint32_t>(c->evOff)};
+  CK(bucket_events(in, ptr<unsigned long long>(c->raw_scratch), E, (uint32_t)n, out, c->st, nullptr));
+  CK(cudaStreamSynchronize(c->st));
+  c->E = E;
+  c->L = L;
+  c->nHits = n;
+  c->maxLayerHits = raw.maxLayerHits;
+  c->haveHits = true;
+  c->stage = 0;
+  sizes->n_hits = n;
+  sizes->n_events = E;
+  sizes->n_layers = L;
+  sizes->n_findable = raw.findableId.size();
+  const size_t nf = std::min<size_t>(raw.findableId.size(), findable_cap);
+  if (findable_id && nf) std::memcpy(findable_id, raw.findableId.data(), nf * 4);
+  if (findable_event && nf) std::memcpy(findable_event, raw.findableEvent.data(), nf * 4);
   return TRAX_OK;
 }
 

@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "trax/trax.h"
+#include "trax_events.h"
 
 struct trax_event_set;
 
@@ -182,9 +183,14 @@ struct Loaded {
   uint32_t nLayers = 0;
 };
 
-// HitCollection::addEvent (HitCollection.cpp:21-180) for one event.
-void add_event(const PEvent& ev, uint32_t evtInGroup, const std::set<uint32_t>& usedLayers, uint32_t maxLayer,
-               float minPt, int numTracks, bool onlyTracks, Loaded& out) {
+// HitCollection::addEvent (HitCollection.cpp:21-180) for one event, as a
+// walk: place(layer, hit) for every hit the reference pushes into its layer
+// bucket, in push order (layers 1 .. maxLayer only: the others are never
+// read out), and found(track id) for every findable track.  The hit
+// collection is the buckets read out layer by layer, each in push order.
+template <class Place, class Found>
+void add_event_walk(const PEvent& ev, const std::set<uint32_t>& usedLayers, uint32_t maxLayer, float minPt,
+                    int numTracks, bool onlyTracks, Place place, Found found) {
   // hits of each simulated track above the minimum pT (:45-57)
   std::map<uint64_t, std::vector<const PHit*>> allTracks;
   for (const PHit& h : ev.hits) {
@@ -196,7 +202,8 @@ void add_event(const PEvent& ev, uint32_t evtInGroup, const std::set<uint32_t>& 
   for (auto& t : allTracks)
     std::stable_sort(t.second.begin(), t.second.end(),
                      [](const PHit* a, const PHit* b) { return a->layer < b->layer; });
-  std::map<uint64_t, std::vector<const PHit*>> layers, findable;
+  std::vector<const std::vector<const PHit*>*> findable;
+  std::vector<uint64_t> findableIds;
   int foundTracks = 0;
   for (auto it = allTracks.begin(); it != allTracks.end() && foundTracks != numTracks; ++it) {
     if (onlyTracks && it->first == 0) continue;
@@ -209,30 +216,44 @@ void add_event(const PEvent& ev, uint32_t evtInGroup, const std::set<uint32_t>& 
     for (uint32_t l : usedLayers)
       if (!cov[l - 1]) missing = true;
     if (it->second[0]->simTrackPt < minPt) continue;
-    for (const PHit* h : it->second) {
-      if (!missing) findable[it->first].push_back(h);
-      else if (!onlyTracks) layers[h->layer].push_back(h);
+    if (!missing) {
+      findable.push_back(&it->second);
+      findableIds.push_back(it->first);
+      ++foundTracks;
+    } else if (!onlyTracks) {
+      for (const PHit* h : it->second)
+        if (h->layer >= 1 && h->layer <= maxLayer) place((uint32_t)h->layer, h);
     }
-    if (!missing) ++foundTracks;
   }
   // findable tracks' hits after the others, layer by layer (:112-120)
-  for (const auto& t : findable)
-    for (const PHit* h : t.second)
-      if (h->layer <= maxLayer) layers[h->layer].push_back(h);
-  // supplements and the hits in layer order (:122-149)
+  for (const auto* t : findable)
+    for (const PHit* h : *t)
+      if (h->layer >= 1 && h->layer <= maxLayer) place((uint32_t)h->layer, h);
+  for (uint64_t id : findableIds) found(id);
+}
+
+// The loader's output for one event: the buckets read out layer by layer
+// (:122-149).
+void add_event(const PEvent& ev, uint32_t evtInGroup, const std::set<uint32_t>& usedLayers, uint32_t maxLayer,
+               float minPt, int numTracks, bool onlyTracks, Loaded& out) {
+  std::vector<std::vector<const PHit*>> layers(maxLayer + 1);
+  add_event_walk(
+      ev, usedLayers, maxLayer, minPt, numTracks, onlyTracks,
+      [&](uint32_t l, const PHit* h) { layers[l].push_back(h); },
+      [&](uint64_t id) {
+        out.findableId.push_back((uint32_t)id);
+        out.findableEvent.push_back(evtInGroup);
+      });
   uint32_t inEvent = 0;
   for (uint32_t l = 1; l <= maxLayer; ++l) {
-    const auto it = layers.find(l);
-    const uint32_t n = it == layers.end() ? 0u : (uint32_t)it->second.size();
+    const uint32_t n = (uint32_t)layers[l].size();
     out.layerHits.push_back(n);
     out.layerOffsets.push_back(inEvent);
     inEvent += n;
   }
   out.eventOffsets.push_back((uint32_t)out.x.size());
-  for (uint32_t l = 1; l <= maxLayer; ++l) {
-    const auto it = layers.find(l);
-    if (it == layers.end()) continue;
-    for (const PHit* h : it->second) {
+  for (uint32_t l = 1; l <= maxLayer; ++l)
+    for (const PHit* h : layers[l]) {
       out.x.push_back(h->x);
       out.y.push_back(h->y);
       out.z.push_back(h->z);
@@ -241,11 +262,6 @@ void add_event(const PEvent& ev, uint32_t evtInGroup, const std::set<uint32_t>& 
       out.hid.push_back((uint32_t)h->simTrackID);  // the HitId column carries the simulated track id
       out.evt.push_back(evtInGroup);
     }
-  }
-  for (const auto& t : findable) {
-    out.findableId.push_back((uint32_t)t.first);
-    out.findableEvent.push_back(evtInGroup);
-  }
 }
 
 template <class T>
@@ -284,6 +300,79 @@ struct Record {
 struct trax_event_set {
   std::vector<PEvent> events;
 };
+
+namespace {
+
+// the layers the layer triplets use, and the highest of them
+int used_layers(const trax_layer_triplet* lt, int n_lt, std::set<uint32_t>& used, uint32_t& maxLayer) {
+  maxLayer = 0;
+  for (int p = 0; p < n_lt; ++p) {
+    for (uint32_t l : {lt[p].layer1, lt[p].layer2, lt[p].layer3}) {
+      if (l == 0) return TRAX_ERR_ARG;
+      used.insert(l);
+    }
+    maxLayer = std::max(maxLayer, lt[p].layer3);
+  }
+  return TRAX_OK;
+}
+
+}  // namespace
+
+namespace trax {
+
+int classify_events(const trax_event_set* s, uint64_t first, uint64_t count, const trax_layer_triplet* lt, int n_lt,
+                    float min_pt, int num_tracks, int only_tracks, RawEvents& out) {
+  if (!s || !lt || n_lt <= 0 || first > s->events.size()) return TRAX_ERR_ARG;
+  const uint64_t last = std::min<uint64_t>(s->events.size(), first + count);
+  std::set<uint32_t> used;
+  uint32_t maxLayer = 0;
+  if (used_layers(lt, n_lt, used, maxLayer) != TRAX_OK) return TRAX_ERR_ARG;
+  out = RawEvents();
+  out.nLayers = maxLayer;
+  for (uint64_t e = first; e < last; ++e) {
+    const PEvent& ev = s->events[e];
+    if (ev.hits.size() >= EVENT_HITS_MAX) return TRAX_ERR_ARG;
+    const size_t base = out.x.size();
+    if (base + ev.hits.size() > 0xffffffffull) return TRAX_ERR_ARG;
+    out.rawOffsets.push_back((uint32_t)base);
+    for (const PHit& h : ev.hits) {
+      out.x.push_back(h.x);
+      out.y.push_back(h.y);
+      out.z.push_back(h.z);
+      out.layer.push_back((uint32_t)h.layer);
+      out.det.push_back((uint32_t)h.detectorId);
+      out.tid.push_back((uint32_t)h.simTrackID);
+      out.key.push_back(EVENT_HIT_DROPPED);
+    }
+    const uint32_t evtInGroup = (uint32_t)(e - first);
+    std::vector<uint32_t> perLayer(maxLayer + 1, 0);
+    uint32_t pushed = 0;
+    add_event_walk(
+        ev, used, maxLayer, min_pt, num_tracks, only_tracks != 0,
+        [&](uint32_t l, const PHit* h) {
+          const uint32_t local = (uint32_t)(h - ev.hits.data());
+          out.key[base + local] = event_hit_key(l, pushed++, local);
+          ++perLayer[l];
+        },
+        [&](uint64_t id) {
+          out.findableId.push_back((uint32_t)id);
+          out.findableEvent.push_back(evtInGroup);
+        });
+    out.eventOffsets.push_back((uint32_t)out.nHits);
+    uint32_t inEvent = 0;
+    for (uint32_t l = 1; l <= maxLayer; ++l) {
+      out.layerHits.push_back(perLayer[l]);
+      out.layerOffsets.push_back(inEvent);
+      inEvent += perLayer[l];
+      out.maxLayerHits = std::max(out.maxLayerHits, perLayer[l]);
+    }
+    out.nHits += pushed;
+  }
+  out.rawOffsets.push_back((uint32_t)out.x.size());
+  return out.nHits > 0xffffffffull ? TRAX_ERR_ARG : TRAX_OK;
+}
+
+}  // namespace trax
 
 extern "C" {
 
@@ -354,13 +443,7 @@ int trax_events_load(const trax_event_set* s, uint64_t first, uint64_t count, co
   const uint64_t last = std::min<uint64_t>(s->events.size(), first + count);
   std::set<uint32_t> used;
   uint32_t maxLayer = 0;
-  for (int p = 0; p < n_lt; ++p) {
-    for (uint32_t l : {lt[p].layer1, lt[p].layer2, lt[p].layer3}) {
-      if (l == 0) return TRAX_ERR_ARG;
-      used.insert(l);
-    }
-    maxLayer = std::max(maxLayer, lt[p].layer3);
-  }
+  if (used_layers(lt, n_lt, used, maxLayer) != TRAX_OK) return TRAX_ERR_ARG;
   Loaded out;
   out.nLayers = maxLayer;
   for (uint64_t e = first; e < last; ++e)

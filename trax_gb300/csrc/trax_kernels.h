@@ -23,6 +23,38 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const 
                            bool flagOverflow);
 cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* launches);
 
+// ------------------------------------------------------ event bucketing
+// The hits of a group of events as their file holds them, with the host's
+// bucketing keys (trax_events.h); scratchOffsets[e]: the event's global
+// sort scratch (events too large for shared memory).
+struct RawEventHits {
+  const float* x;
+  const float* y;
+  const float* z;
+  const uint32_t* layer;
+  const uint32_t* det;
+  const uint32_t* tid;
+  const unsigned long long* key;
+  const uint32_t* rawOffsets;      // [E+1]
+  const uint32_t* scratchOffsets;  // [E]
+};
+// the context's input hit columns and the first kept hit of each event
+struct HitColumns {
+  float* x;
+  float* y;
+  float* z;
+  uint32_t* layer;
+  uint32_t* det;
+  uint32_t* hid;
+  uint32_t* evt;
+  const uint32_t* eventOffsets;  // [E]
+};
+// global scratch keys an event of this many hits needs (0: shared memory)
+uint32_t bucket_scratch_keys(uint32_t hitsInEvent);
+// every event's kept hits, sorted by key, into the columns at its offset
+cudaError_t bucket_events(const RawEventHits& in, unsigned long long* scratch, uint32_t nEvents, uint32_t nKept,
+                          HitColumns out, cudaStream_t st, uint32_t* launches);
+
 // ------------------------------------------------------------ grid build
 struct GridInput {
   const float* x;

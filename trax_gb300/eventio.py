@@ -1,7 +1,9 @@
 """Event files (PEventContainer) and the reference's event loader, through the
-C ABI (trax_events_read / trax_events_raw / trax_events_load): the hits of a
-file become an EventBatch like the synthetic workloads', plus the findable
-tracks the physics metrics count against."""
+C ABI (trax_events_read / trax_events_raw / trax_events_load, and
+trax_events_upload with the layer bucketing on the device): the hits of a
+file become an EventBatch like the synthetic workloads', or the hits of a
+context directly, plus the findable tracks the physics metrics count
+against."""
 from __future__ import annotations
 
 import ctypes
@@ -105,6 +107,30 @@ class EventFile:
             layer_offsets=lay_off, min_r=np.asarray(min_r, np.float32), max_r=np.asarray(max_r, np.float32),
             lts=list(lts), n_z=n_z, n_phi=n_phi, min_pt=min_pt, d_eta_cut=events.D_ETA_CUT)
         return batch, fid, fev
+
+    def upload(self, ctx: "capi.Context", lts: List[events.LayerTriplet], min_pt: float, first: int = 0,
+               count: Optional[int] = None, num_tracks: int = -1, only_tracks: bool = False):
+        """The loader with its layer bucketing on the device (trax_events_upload):
+        the context's hits become those of `load` without a host-side copy of
+        the reordered columns.  The context's layer triplets, geometry and grid
+        are set by the caller.  Returns (sizes, findable track ids, their
+        events)."""
+        count = self.n_events - first if count is None else count
+        lt = (capi.LayerTripletC * len(lts))(*[capi.LayerTripletC(
+            t.layer1, t.layer2, t.layer3, t.dtheta_cut, t.sigma_z, t.dphi_cut, t.sigma_phi, t.tip_cut,
+            t.pair_spread_z, t.z0, t.pair_spread_phi, t.n_candidates) for t in lts])
+        sz = LoadedSizesC()
+        cap = 1 << 20
+        fid = np.zeros(cap, np.uint32)
+        fev = np.zeros(cap, np.uint32)
+        ctx._check(self._L.trax_events_upload(ctx._h, self._h, first, count, lt, len(lts), ctypes.c_float(min_pt),
+                                               num_tracks, int(only_tracks), ctypes.byref(sz), _p(fid), _p(fev),
+                                               cap))
+        H, E, L, F = (int(getattr(sz, k)) for k in ("n_hits", "n_events", "n_layers", "n_findable"))
+        ctx.n_events, ctx.n_layers, ctx.n_hits = E, L, H
+        if F > cap:
+            raise capi.TraxError(capi.TRAX_ERR_CAPACITY, f"{F} findable tracks, more than {cap}")
+        return {"n_hits": H, "n_events": E, "n_layers": L, "n_findable": F}, fid[:F].copy(), fev[:F].copy()
 
     def _check(self, rc):
         if rc != capi.TRAX_OK:
