@@ -371,6 +371,15 @@ int trax_physics_triplets(const uint32_t* h1, const uint32_t* h2, const uint32_t
                           uint32_t n_events, uint32_t n_lt, const uint32_t* hit_track_id, const uint32_t* findable_id,
                           const uint32_t* findable_event, uint64_t n_findable, trax_physics_record* out);
 
+/* The same records for the context's current triplets, counted on the
+ * device: fake and real triplets and the distinct findable tracks found per
+ * (event, layer triplet) are counted by kernels over the triplets and the
+ * grid-ordered hit ids left on the device; only those counts come back for
+ * the means and deviations.  Equal to trax_physics_triplets on the
+ * downloaded triplets with the grid-ordered hit ids. */
+int trax_physics_triplets_device(trax_ctx* ctx, const uint32_t* findable_id, const uint32_t* findable_event,
+                                 uint64_t n_findable, trax_physics_record* out);
+
 /* Track evaluation of TripletBuilder.cpp:840-1066: tracks of three or more
  * triplets from the CA output (trax_get_tracks), clone removal (tracks that
  * share at least 19 % of the shorter one's hits), real tracks (all hits of

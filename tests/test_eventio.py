@@ -280,6 +280,7 @@ def test_loaded_events_on_the_gpu_match_the_oracle(eventio, oracle_lib, tmp_path
         ctx.upload(batch)
         ctx.seed_batch(use_graph=True)
         got = ctx.results()
+        on_device = physics.triplet_records_device(ctx, fid, fev)
     finally:
         ctx.close()
     for k in ("perm", "pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "trip_offsets"):
@@ -290,6 +291,8 @@ def test_loaded_events_on_the_gpu_match_the_oracle(eventio, oracle_lib, tmp_path
     b = physics.triplet_records(ref["trip_h1"], ref["trip_h2"], ref["trip_h3"], ref["trip_offsets"],
                                 batch.n_events, len(lts), hid, fid, fev)
     assert a == b
+    # the same records counted on the device from the context's triplets
+    assert on_device == a
 
 
 @pytest.mark.gpu
@@ -299,7 +302,7 @@ def test_device_bucketing_matches_host_loader(eventio, tmp_path, num_tracks, onl
     as trax_events_load + trax_upload_hits do: the same chain results
     element by element and the same findable tracks.  The last event has more
     than 4 096 hits, so its keys sort in global scratch."""
-    from trax_gb300 import capi
+    from trax_gb300 import capi, physics
     p = tmp_path / "events.pb"
     evs = synthetic_events(seed=11, n_events=5) + synthetic_events(seed=12, n_events=1, n_tracks=700)
     for ev in evs:  # radii per layer, as in the test above
@@ -323,10 +326,14 @@ def test_device_bucketing_matches_host_loader(eventio, tmp_path, num_tracks, onl
         sizes, fid2, fev2 = f.upload(b, lts, 1.0, num_tracks=num_tracks, only_tracks=only_tracks)
         b.seed_batch(use_graph=True)
         rb = b.results()
+        phys_dev = physics.triplet_records_device(b, fid2, fev2)
     finally:
         a.close()
         b.close()
     assert (sizes["n_hits"], sizes["n_events"]) == (batch.n_hits, batch.n_events)
+    hid = batch.hit_id[ra["perm"]]
+    assert phys_dev == physics.triplet_records(ra["trip_h1"], ra["trip_h2"], ra["trip_h3"], ra["trip_offsets"],
+                                               batch.n_events, len(lts), hid, fid, fev)
     assert np.array_equal(fid, fid2) and np.array_equal(fev, fev2)
     assert ra["pairs"].size > 0
     if num_tracks < 0:

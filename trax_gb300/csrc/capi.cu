@@ -114,6 +114,8 @@ struct trax_ctx {
   DevBuf in_x, in_y, in_z, in_layer, in_det, in_hid, in_evt, evOff, layHits, layOff;
   // event-file hits for the device bucketing (trax_events_upload)
   DevBuf raw_x, raw_y, raw_z, raw_layer, raw_det, raw_tid, raw_key, raw_off, raw_scratchOff, raw_scratch;
+  // triplet physics counts (trax_physics_triplets_device)
+  DevBuf phys_findOff, phys_findIds, phys_flags, phys_counts;
   // grid stage
   DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
   // pair stage
@@ -917,7 +919,8 @@ void trax_destroy(trax_ctx* c) {
   drop_graph(c);
   DevBuf* bufs[] = {&c->in_x, &c->in_y, &c->in_z, &c->in_layer, &c->in_det, &c->in_hid, &c->in_evt, &c->evOff,
                     &c->layHits, &c->layOff, &c->raw_x, &c->raw_y, &c->raw_z, &c->raw_layer, &c->raw_det,
-                    &c->raw_tid, &c->raw_key, &c->raw_off, &c->raw_scratchOff, &c->raw_scratch, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
+                    &c->raw_tid, &c->raw_key, &c->raw_off, &c->raw_scratchOff, &c->raw_scratch, &c->phys_findOff,
+                    &c->phys_findIds, &c->phys_flags, &c->phys_counts, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
                     &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
@@ -1370,6 +1373,51 @@ int trax_get_triplets(trax_ctx* c, uint32_t* h1, uint32_t* h2, uint32_t* h3, uin
   RC(copy_out(c, h3, c->h3, c->nT * 4));
   RC(copy_out(c, offsets, c->tripOffsets, ((size_t)c->cfg.E * c->cfg.nLT + 1) * 4));
   CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_physics_triplets_device(trax_ctx* c, const uint32_t* findable_id, const uint32_t* findable_event,
+                                 uint64_t n_findable, trax_physics_record* out) {
+  if (!c || !out || (n_findable && (!findable_id || !findable_event))) return fail(c, TRAX_ERR_ARG, "null argument");
+  if (c->stage < 4) return fail(c, TRAX_ERR_STATE, "triplets not filtered");
+  if (c->identityHits) return fail(c, TRAX_ERR_STATE, "the hits of caller triplets carry no grid order");
+  const Mode mode = SYNCED;
+  const uint32_t E = c->cfg.E, nLT = c->cfg.nLT;
+  const size_t S = (size_t)E * nLT;
+  // each event's findable track ids, sorted and distinct (the truth sets)
+  std::vector<std::pair<uint32_t, uint32_t>> truth;
+  for (uint64_t k = 0; k < n_findable; ++k)
+    if (findable_event[k] < E) truth.emplace_back(findable_event[k], findable_id[k]);
+  std::sort(truth.begin(), truth.end());
+  truth.erase(std::unique(truth.begin(), truth.end()), truth.end());
+  std::vector<uint32_t> findOff(E + 1, 0), findIds(truth.size()), truthSize(E, 0);
+  for (size_t k = 0; k < truth.size(); ++k) {
+    findIds[k] = truth[k].second;
+    ++truthSize[truth[k].first];
+  }
+  for (uint32_t e = 0; e < E; ++e) findOff[e + 1] = findOff[e] + truthSize[e];
+  ENSURE(phys_findOff, E + 1, 4);
+  ENSURE(phys_findIds, std::max<size_t>(findIds.size(), 1), 4);
+  ENSURE(phys_flags, std::max<size_t>(nLT * findIds.size(), 1), 4);
+  ENSURE(phys_counts, 3 * S + 1, 4);
+  CK(cudaMemcpyAsync(c->phys_findOff.p, findOff.data(), (size_t)(E + 1) * 4, cudaMemcpyHostToDevice, c->st));
+  if (!findIds.empty())
+    CK(cudaMemcpyAsync(c->phys_findIds.p, findIds.data(), findIds.size() * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->phys_flags.p, 0, std::max<size_t>(nLT * findIds.size(), 1) * 4, c->st));
+  CK(cudaMemsetAsync(c->phys_counts.p, 0, (3 * S + 1) * 4, c->st));
+  uint32_t* counts = ptr<uint32_t>(c->phys_counts);
+  CK(physics_counts(ptr<uint32_t>(c->h1), ptr<uint32_t>(c->h2), ptr<uint32_t>(c->h3), slot(c, S_TRIPLETS), c->nT,
+                    ptr<uint32_t>(c->tripOffsets), ptr<uint32_t>(c->phid), E, nLT, ptr<uint32_t>(c->phys_findOff),
+                    ptr<uint32_t>(c->phys_findIds), counts,
+                    counts + S, ptr<uint32_t>(c->phys_flags), counts + 2 * S, c->st, nullptr));
+  std::vector<uint32_t> h(3 * S), offsets(S + 1);
+  if (S) CK(cudaMemcpyAsync(h.data(), counts, 3 * S * 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(offsets.data(), c->tripOffsets.p, (S + 1) * 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  // clones: real triplets of findable tracks beyond the first per track
+  std::vector<uint32_t> clones(S);
+  for (size_t k = 0; k < S; ++k) clones[k] = h[S + k] - h[2 * S + k];
+  trax::physics_records(E, nLT, offsets.data(), h.data() + 2 * S, h.data(), clones.data(), truthSize.data(), out);
   return TRAX_OK;
 }
 

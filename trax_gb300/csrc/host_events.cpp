@@ -372,6 +372,43 @@ int classify_events(const trax_event_set* s, uint64_t first, uint64_t count, con
   return out.nHits > 0xffffffffull ? TRAX_ERR_ARG : TRAX_OK;
 }
 
+void physics_records(uint32_t n_events, uint32_t n_lt, const uint32_t* offsets, const uint32_t* found,
+                     const uint32_t* fakes, const uint32_t* clones, const uint32_t* truthSize,
+                     trax_physics_record* out) {
+  std::vector<Record> perLT(n_lt);
+  std::vector<bool> seen(n_lt, false);
+  for (uint32_t e = 0; e < n_events; ++e)
+    for (uint32_t p = 0; p < n_lt; ++p) {
+      const size_t seg = (size_t)e * n_lt + p;
+      const uint32_t a = offsets[seg], b = offsets[seg + 1];
+      const double nFound = b > a ? (double)(b - a) : 0.0;
+      Record r;
+      r.lt = p;
+      r.n = 1;
+      r.eff.mean = (double)found[seg] / std::max<double>((double)truthSize[e], 1.0);
+      r.fake.mean = (double)fakes[seg] / std::max(nFound, 1.0);
+      r.clone.mean = (double)clones[seg] / std::max(nFound, 1.0);
+      // PhysicsRecords::addRecord (:360-371): merge by layer triplet
+      if (!seen[p]) {
+        perLT[p] = r;
+        seen[p] = true;
+      } else {
+        perLT[p].merge(r);
+      }
+    }
+  // csvDump (:380-404): every layer triplet, then the total over them
+  for (uint32_t p = 0; p < n_lt; ++p) {
+    const Record& r = perLT[p];
+    out[p] = trax_physics_record{p, (uint64_t)r.n, r.eff.mean, r.dev(r.eff), r.fake.mean, r.dev(r.fake),
+                                 r.clone.mean, r.dev(r.clone)};
+  }
+  Record total = perLT[0];
+  for (uint32_t p = 1; p < n_lt; ++p) total.merge(perLT[p]);
+  out[n_lt] = trax_physics_record{n_lt + 1, (uint64_t)total.n, total.eff.mean, total.dev(total.eff),
+                                  total.fake.mean, total.dev(total.fake), total.clone.mean,
+                                  total.dev(total.clone)};
+}
+
 }  // namespace trax
 
 extern "C" {
@@ -502,50 +539,28 @@ int trax_physics_triplets(const uint32_t* h1, const uint32_t* h2, const uint32_t
   std::vector<std::set<uint32_t>> truth(n_events);
   for (uint64_t k = 0; k < n_findable; ++k)
     if (findable_event[k] < n_events) truth[findable_event[k]].insert(findable_id[k]);
-  std::vector<Record> perLT(n_lt);
-  std::vector<bool> seen(n_lt, false);
-  for (uint32_t e = 0; e < n_events; ++e)
+  const size_t S = (size_t)n_events * n_lt;
+  std::vector<uint32_t> found(S), fakes(S), clones(S), truthSize(n_events);
+  for (uint32_t e = 0; e < n_events; ++e) {
+    truthSize[e] = (uint32_t)truth[e].size();
     for (uint32_t p = 0; p < n_lt; ++p) {
       // PhysicsRecord::fillData (PhysicsRecord.cpp:86-313) for (e, p)
-      const uint32_t a = offsets[(size_t)e * n_lt + p], b = offsets[(size_t)e * n_lt + p + 1];
-      std::set<uint32_t> found;
-      uint64_t fakes = 0, clones = 0;
-      for (uint32_t t = a; t < b; ++t) {
+      const size_t seg = (size_t)e * n_lt + p;
+      std::set<uint32_t> seen;
+      for (uint32_t t = offsets[seg]; t < offsets[seg + 1]; ++t) {
         const uint32_t i1 = hit_track_id[h1[t]], i2 = hit_track_id[h2[t]], i3 = hit_track_id[h3[t]];
         if (i1 == i2 && i1 == i3) {
           if (truth[e].count(i1)) {
-            if (!found.insert(i1).second) ++clones;
+            if (!seen.insert(i1).second) ++clones[seg];
           }
         } else {
-          ++fakes;
+          ++fakes[seg];
         }
       }
-      const double nFound = b > a ? (double)(b - a) : 0.0;
-      Record r;
-      r.lt = p;
-      r.n = 1;
-      r.eff.mean = (double)found.size() / std::max<double>((double)truth[e].size(), 1.0);
-      r.fake.mean = (double)fakes / std::max(nFound, 1.0);
-      r.clone.mean = (double)clones / std::max(nFound, 1.0);
-      // PhysicsRecords::addRecord (:360-371): merge by layer triplet
-      if (!seen[p]) {
-        perLT[p] = r;
-        seen[p] = true;
-      } else {
-        perLT[p].merge(r);
-      }
+      found[seg] = (uint32_t)seen.size();
     }
-  // csvDump (:380-404): every layer triplet, then the total over them
-  for (uint32_t p = 0; p < n_lt; ++p) {
-    const Record& r = perLT[p];
-    out[p] = trax_physics_record{p, (uint64_t)r.n, r.eff.mean, r.dev(r.eff), r.fake.mean, r.dev(r.fake),
-                                 r.clone.mean, r.dev(r.clone)};
   }
-  Record total = perLT[0];
-  for (uint32_t p = 1; p < n_lt; ++p) total.merge(perLT[p]);
-  out[n_lt] = trax_physics_record{n_lt + 1, (uint64_t)total.n, total.eff.mean, total.dev(total.eff),
-                                  total.fake.mean, total.dev(total.fake), total.clone.mean,
-                                  total.dev(total.clone)};
+  trax::physics_records(n_events, n_lt, offsets, found.data(), fakes.data(), clones.data(), truthSize.data(), out);
   return TRAX_OK;
 }
 

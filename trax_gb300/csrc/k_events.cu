@@ -1,4 +1,5 @@
-// k_events.cu -- the loader's layer bucketing on the device.
+// k_events.cu -- the loader's layer bucketing and the triplet physics counts
+// on the device.
 //
 // HitCollection::addEvent (HitCollection.cpp:21-180) ends by reading its
 // layer buckets out, layer by layer, each in push order, into the hit
@@ -8,6 +9,8 @@
 // shared memory up to BUCKET_SMEM_KEYS keys, else in global scratch) and
 // gathers the kept hits' columns into the context's input arrays at the
 // event's offset.  Keys are distinct, so the sort needs no stability.
+#include <algorithm>
+
 #include "trax_kernels.h"
 
 namespace trax {
@@ -60,7 +63,84 @@ __global__ void __launch_bounds__(BUCKET_THREADS)
   }
 }
 
+// PhysicsRecord::fillData (PhysicsRecord.cpp:86-313) counted per triplet:
+// a triplet whose three hits carry one simulated track id is real, else fake;
+// a real triplet of a findable track (binary search in its event's sorted
+// findable ids) marks that track found in its segment.  The segments are the
+// triplet offsets' ranges, as fillData reads them: the reference's offsets
+// leave the last triplet out of every range (filterOffsetStore), and so does
+// this count.
+__global__ void physics_triplet_kernel(const uint32_t* __restrict__ h1, const uint32_t* __restrict__ h2,
+                                       const uint32_t* __restrict__ h3, const uint32_t* nTDev,
+                                       const uint32_t* __restrict__ offsets, uint32_t S,
+                                       const uint32_t* __restrict__ hitTrack, uint32_t nLT,
+                                       const uint32_t* __restrict__ findOff, const uint32_t* __restrict__ findIds,
+                                       uint32_t* fakes, uint32_t* realFindable, uint32_t* foundFlags) {
+  const uint32_t nT = *nTDev;
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nT; t += gridDim.x * blockDim.x) {
+    // the segment whose range holds t: the last s with offsets[s] <= t
+    uint32_t lo = 0, hi = S + 1;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (offsets[mid] <= t) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo == 0 || lo > S) continue;  // before the first range, or at or past offsets[S]
+    const uint32_t seg = lo - 1;
+    const uint32_t e = seg / nLT, p = seg % nLT;
+    const uint32_t i1 = hitTrack[h1[t]], i2 = hitTrack[h2[t]], i3 = hitTrack[h3[t]];
+    if (i1 != i2 || i1 != i3) {
+      atomicAdd(&fakes[seg], 1u);
+      continue;
+    }
+    lo = findOff[e];
+    hi = findOff[e + 1];
+    const uint32_t f0 = lo, nf = hi - lo;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (findIds[mid] < i1) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo < f0 + nf && findIds[lo] == i1) {
+      atomicAdd(&realFindable[seg], 1u);
+      foundFlags[(size_t)nLT * f0 + (size_t)p * nf + (lo - f0)] = 1u;
+    }
+  }
+}
+
+// distinct findable tracks found per segment
+__global__ void physics_found_kernel(uint32_t S, uint32_t nLT, const uint32_t* __restrict__ findOff,
+                                     const uint32_t* __restrict__ foundFlags, uint32_t* found) {
+  for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < S; s += gridDim.x * blockDim.x) {
+    const uint32_t e = s / nLT, p = s % nLT;
+    const uint32_t f0 = findOff[e], nf = findOff[e + 1] - f0;
+    const uint32_t* fl = foundFlags + (size_t)nLT * f0 + (size_t)p * nf;
+    uint32_t n = 0;
+    for (uint32_t q = 0; q < nf; ++q) n += fl[q];
+    found[s] = n;
+  }
+}
+
 }  // namespace
+
+cudaError_t physics_counts(const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, const uint32_t* nTDev,
+                           uint64_t maxT, const uint32_t* offsets, const uint32_t* hitTrack, uint32_t nEvents,
+                           uint32_t nLT, const uint32_t* findOff,
+                           const uint32_t* findIds, uint32_t* fakes, uint32_t* realFindable, uint32_t* foundFlags,
+                           uint32_t* found, cudaStream_t st, uint32_t* launches) {
+  const uint32_t S = nEvents * nLT;
+  if (maxT > 0) {
+    const uint64_t b = std::min<uint64_t>((maxT + 255) / 256, 4096);
+    physics_triplet_kernel<<<(unsigned)b, 256, 0, st>>>(h1, h2, h3, nTDev, offsets, S, hitTrack, nLT, findOff,
+                                                        findIds, fakes, realFindable, foundFlags);
+    if (launches) *launches += 1;
+  }
+  if (S > 0) {
+    physics_found_kernel<<<(S + 255) / 256, 256, 0, st>>>(S, nLT, findOff, foundFlags, found);
+    if (launches) *launches += 1;
+  }
+  return cudaGetLastError();
+}
 
 uint32_t bucket_scratch_keys(uint32_t hitsInEvent) {
   uint32_t padded = 1;

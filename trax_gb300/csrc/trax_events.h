@@ -1,5 +1,6 @@
 // trax_events.h -- event-file hits classified on the host for the device
-// bucketing step of trax_events_upload.
+// bucketing step of trax_events_upload, and the physics records shared by
+// the host and device counting.
 //
 // HitCollection::addEvent (HitCollection.cpp:21-180) decides per hit whether
 // the loader keeps it (its track's pT, findability, the track limit) and in
@@ -44,5 +45,13 @@ struct RawEvents {
 // TRAX_ERR_ARG (bad arguments, an event of EVENT_HITS_MAX hits or more)
 int classify_events(const trax_event_set* events, uint64_t first, uint64_t count, const trax_layer_triplet* lt,
                     int n_lt, float min_pt, int num_tracks, int only_tracks, RawEvents& out);
+
+// PhysicsRecord's means and deviations (PhysicsRecord.cpp:86-404) from the
+// counts of every (event, layer triplet) segment: distinct findable tracks
+// found, fake triplets, clone triplets; truthSize: findable tracks per event.
+// out [n_lt + 1]: every layer triplet, then the total.
+void physics_records(uint32_t n_events, uint32_t n_lt, const uint32_t* offsets, const uint32_t* found,
+                     const uint32_t* fakes, const uint32_t* clones, const uint32_t* truthSize,
+                     trax_physics_record* out);
 
 }  // namespace trax

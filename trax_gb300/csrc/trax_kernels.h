@@ -55,6 +55,17 @@ uint32_t bucket_scratch_keys(uint32_t hitsInEvent);
 cudaError_t bucket_events(const RawEventHits& in, unsigned long long* scratch, uint32_t nEvents, uint32_t nKept,
                           HitColumns out, cudaStream_t st, uint32_t* launches);
 
+// per (event, layer triplet) segment of the triplet offsets [S+1]: fake
+// triplets, real
+// triplets of findable tracks, distinct findable tracks found; findIds are
+// each event's findable track ids, sorted, from findOff[e]; foundFlags
+// [nLT * n_findable] zeroed by the caller, as are fakes and realFindable
+cudaError_t physics_counts(const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, const uint32_t* nTDev,
+                           uint64_t maxT, const uint32_t* offsets, const uint32_t* hitTrack, uint32_t nEvents,
+                           uint32_t nLT, const uint32_t* findOff,
+                           const uint32_t* findIds, uint32_t* fakes, uint32_t* realFindable, uint32_t* foundFlags,
+                           uint32_t* found, cudaStream_t st, uint32_t* launches);
+
 // ------------------------------------------------------------ grid build
 struct GridInput {
   const float* x;

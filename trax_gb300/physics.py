@@ -1,5 +1,5 @@
-"""Physics bookkeeping of seeding results (trax_physics_triplets /
-trax_physics_tracks): triplet efficiency, fake and clone rates per layer
+"""Physics bookkeeping of seeding results (trax_physics_triplets, counted on the
+host or, for a context's triplets, on the device; trax_physics_tracks): triplet efficiency, fake and clone rates per layer
 triplet as the reference's PhysicsRecord, and the track-level evaluation of
 its triplet builder."""
 from __future__ import annotations
@@ -38,6 +38,16 @@ def triplet_records(h1, h2, h3, offsets, n_events: int, n_lt: int, hit_track_id,
                                  arrs[6].ctypes.data, arrs[5].size, out)
     if rc != capi.TRAX_OK:
         raise capi.TraxError(rc, "trax_physics_triplets failed")
+    return [{f[0]: getattr(r, f[0]) for f in PhysicsRecordC._fields_} for r in out]
+
+
+def triplet_records_device(ctx: "capi.Context", findable_id, findable_event) -> List[Dict[str, float]]:
+    """The same records for the context's current triplets, counted on the device
+    (trax_physics_triplets_device)."""
+    fid, fev = _u32(findable_id), _u32(findable_event)
+    out = (PhysicsRecordC * (ctx.n_lt + 1))()
+    ctx._check(ctx._L.trax_physics_triplets_device(ctx._h, fid.ctypes.data if fid.size else None,
+                                                   fev.ctypes.data if fev.size else None, fid.size, out))
     return [{f[0]: getattr(r, f[0]) for f in PhysicsRecordC._fields_} for r in out]
 
 
