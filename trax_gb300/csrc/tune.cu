@@ -205,8 +205,8 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
       }
     };
     if (searchGrid) {
-      static const uint32_t zs[] = {50, 100, 150, 200, 300, 400};
-      static const uint32_t ps[] = {64, 128, 256};
+      static const uint32_t zs[] = {50, 100, 150, 200, 250, 300, 400};
+      static const uint32_t ps[] = {48, 64, 96, 128, 256};
       for (uint32_t z : zs)
         for (uint32_t p : ps) {
           if ((z + 1) * (p + 1) > TRAX_GRID_SMEM_CELLS) continue;
