@@ -34,6 +34,7 @@
 #include <stdexcept>
 #include <string>
 #include <tuple>
+#include <utility>
 #include <vector>
 
 #include "trax.h"
@@ -295,6 +296,62 @@ inline void buildSupplements(const HitCollection& hits, uint32_t nEvents, uint32
     }
     run += inEvent;
   }
+}
+
+// A PEventContainer file (the reference's Event.proto, PEventStore), read
+// on the host.
+class EventFile {
+ public:
+  explicit EventFile(const std::string& path) {
+    const int rc = trax_events_read(path.c_str(), &set_, &n_);
+    if (rc != TRAX_OK) throw Error(rc, "cannot read event file " + path);
+  }
+  ~EventFile() { trax_events_free(set_); }
+  EventFile(const EventFile&) = delete;
+  EventFile& operator=(const EventFile&) = delete;
+  uint64_t size() const { return n_; }
+  const trax_event_set* handle() const { return set_; }
+
+ private:
+  trax_event_set* set_ = nullptr;
+  uint64_t n_ = 0;
+};
+
+// HitCollection::addEvent (HitCollection.cpp:21-180) for events [first,
+// first + count) of a file, as the reference's loop over a PEventContainer
+// calls it with evtInGroup = 0, 1, ...: the collection and the supplements
+// are replaced by those events' hits; returns the findable (track id, event
+// in the group) pairs, the reference's tTrackList per event.
+inline std::vector<std::pair<uint32_t, uint32_t>> addEvents(const EventFile& file, uint64_t first, uint64_t count,
+                                                            const TripletConfigurations& lts, int numTracks,
+                                                            bool onlyTracks, HitCollection& hits,
+                                                            EventSupplement& es, LayerSupplement& ls) {
+  trax_loaded_sizes sz{};
+  auto load = [&](float* x, float* y, float* z, uint32_t* layer, uint32_t* det, uint32_t* hid, uint32_t* evt,
+                  uint32_t* eo, uint32_t* lh, uint32_t* lo, uint32_t* fid, uint32_t* fev) {
+    const int rc = trax_events_load(file.handle(), first, count, lts.rows().data(), (int)lts.size(), lts.minPt(),
+                                    numTracks, onlyTracks ? 1 : 0, &sz, x, y, z, layer, det, hid, evt, eo, lh, lo,
+                                    fid, fev);
+    if (rc != TRAX_OK) throw Error(rc, "trax_events_load failed");
+  };
+  load(nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+  hits.x.assign(sz.n_hits, 0.0f);
+  hits.y.assign(sz.n_hits, 0.0f);
+  hits.z.assign(sz.n_hits, 0.0f);
+  hits.layer.assign(sz.n_hits, 0u);
+  hits.detId.assign(sz.n_hits, 0u);
+  hits.hitId.assign(sz.n_hits, 0u);
+  hits.event.assign(sz.n_hits, 0u);
+  es.offset.assign(sz.n_events, 0u);
+  ls.nLayers = (uint32_t)sz.n_layers;
+  ls.nHits.assign(sz.n_events * sz.n_layers, 0u);
+  ls.offset.assign(sz.n_events * sz.n_layers, 0u);
+  std::vector<uint32_t> fid(sz.n_findable), fev(sz.n_findable);
+  load(hits.x.data(), hits.y.data(), hits.z.data(), hits.layer.data(), hits.detId.data(), hits.hitId.data(),
+       hits.event.data(), es.offset.data(), ls.nHits.data(), ls.offset.data(), fid.data(), fev.data());
+  std::vector<std::pair<uint32_t, uint32_t>> findable(sz.n_findable);
+  for (size_t k = 0; k < findable.size(); ++k) findable[k] = {fid[k], fev[k]};
+  return findable;
 }
 
 // Pairing (Pairings.h:9-59): (first, second) hit pairs and per-(event,
