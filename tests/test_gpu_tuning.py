@@ -20,7 +20,7 @@ def ctx(trax_lib):
     c.close()
 
 
-@pytest.mark.parametrize("blocks", [(64, 64, 128), (256, 256, 64), (96, 160, 224)])
+@pytest.mark.parametrize("blocks", [(64, 64, 128), (256, 256, 64), (96, 160, 224), (192, 96, 192)])
 def test_block_sizes_keep_results(ctx, oracle_lib, blocks):
     batch = events.generate(2, n_events=3)
     ref = oracle_lib.run(batch)[0]

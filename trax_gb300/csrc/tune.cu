@@ -214,7 +214,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
           consider(Shape{z, p, best.pairT, best.predT, best.filtT});
         }
     }
-    static const uint32_t ts[] = {64, 128, 256};
+    static const uint32_t ts[] = {64, 96, 128, 192, 256};
     for (int k = 0; k < 3; ++k)
       for (uint32_t t : ts) {
         Shape s = best;
