@@ -179,13 +179,20 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells):
 TRAFFIC_PER_UNIT = {  # by grid (nZ x nPhi): the grid changes the cells read and the hits visited
     "150x64": {"predict_count": ("pairs", 32.5), "filter": ("candidates", 27.3), "grid_build": ("hits", 97.0)},
     "200x64": {"predict_count": ("pairs", 32.7), "filter": ("candidates", 27.3), "grid_build": ("hits", 110.9)},
+    "250x48": {"predict_count": ("pairs", 32.6), "filter": ("candidates", 27.2), "grid_build": ("hits", 107.6)},
+    "300x48": {"predict_count": ("pairs", 32.9), "filter": ("candidates", 27.1), "grid_build": ("hits", 118.4)},
+    "250x32": {"predict_count": ("pairs", 32.2), "filter": ("candidates", 27.2), "grid_build": ("hits", 90.4)},
+    "200x48": {"predict_count": ("pairs", 32.4), "filter": ("candidates", 27.2), "grid_build": ("hits", 97.2)},
+    "250x64": {"predict_count": ("pairs", 33.0), "filter": ("candidates", 27.2), "grid_build": ("hits", 125.0)},
 }
 
 
 # warp instructions per unit of work (ncu smsp__inst_executed.sum of the same
 # 300-event capture / its units): the dominant kernels are issue-bound, so
 # their position against the SMs' issue rate is reported beside the HBM one
-INST_PER_UNIT = {"150x64": {"predict_count": ("pairs", 30.37)}, "200x64": {"predict_count": ("pairs", 28.76)}}
+INST_PER_UNIT = {g: {"predict_count": ("pairs", v)} for g, v in (
+    ("150x64", 30.37), ("200x64", 28.76), ("250x48", 28.06), ("300x48", 27.29), ("250x32", 28.67),
+    ("200x48", 29.15), ("250x64", 27.73))}
 
 
 def kernel_issue(name, st, ms, clk, device, grid):
