@@ -107,6 +107,48 @@ def test_warp_tile_boundaries(ctx, oracle_lib):
     compare(ctx.results(), ref)
 
 
+def test_full_batch_equals_its_events_run_alone(ctx, oracle_lib):
+    """At the benchmark's full size (1000 events, 9.7 M hits): events are
+    independent, so each event's slice of the batched results equals the
+    oracle's results for that event alone, hit indices shifted by the event's
+    first hit and pair indices by its first pair.  Twelve events are checked
+    that way; over the whole batch the triplet offsets are monotone and every
+    segment's triplets are sorted by (h2, h1) (non-decreasing: a pair can
+    have several third hits)."""
+    batch = events.generate(2)
+    ctx.upload(batch)
+    ctx.seed_batch(use_graph=True)
+    got = ctx.results()
+    n_lt = len(batch.lts)
+    sentinel = np.uint32(0xFFFFFFFF)
+    po, co, to = (np.asarray(got[k]) for k in ("pair_offsets", "cand_offsets", "trip_offsets"))
+    hits_per_event = np.diff(np.append(batch.event_offsets, batch.n_hits))
+    rng = np.random.default_rng(0)
+    small = np.nonzero(hits_per_event[:-1] < 8000)[0]
+    sample = sorted(set(rng.choice(small, 10, replace=False).tolist()) | {0, batch.n_events - 2})
+    for e in sample:
+        ref = oracle_lib.run(batch.subset([e]))[0]
+        off = np.uint32(batch.event_offsets[e])
+        pa, pb = int(po[e * n_lt]), int(po[(e + 1) * n_lt])
+        pairs = np.asarray(got["pairs"])[2 * pa:2 * pb].copy()
+        pairs[pairs != sentinel] -= off
+        assert np.array_equal(pairs, ref["pairs"]), e
+        ca, cb = int(co[e * n_lt]), int(co[(e + 1) * n_lt])
+        cands = np.asarray(got["cands"])[2 * ca:2 * cb].reshape(-1, 2).copy()
+        cands[:, 0] -= np.uint32(pa)
+        cands[cands[:, 1] != sentinel, 1] -= off
+        assert np.array_equal(cands.reshape(-1), ref["cands"]), e
+        ta, tb = int(to[e * n_lt]), int(to[(e + 1) * n_lt])
+        for k in ("trip_h1", "trip_h2", "trip_h3"):
+            assert np.array_equal(np.asarray(got[k])[ta:tb] - off, ref[k]), (e, k)
+    assert np.all(np.diff(to.astype(np.int64)) >= 0)
+    h1, h2 = (np.asarray(got[k]).astype(np.uint64) for k in ("trip_h1", "trip_h2"))
+    key = (h2 << np.uint64(32)) | h1
+    seg = np.searchsorted(to, np.arange(key.size), side="right")
+    same = seg[1:] == seg[:-1]
+    assert np.all(key[1:][same] >= key[:-1][same])  # equal keys: one pair, several third hits
+
+
 def test_batched_synced_matches_graph(ctx, oracle_lib):
     batch = events.generate(2, n_events=4)
     ctx.upload(batch)
