@@ -392,6 +392,12 @@ typedef struct trax_track_metrics {
 int trax_physics_tracks(const uint32_t* tracks, const uint32_t* track_offsets, uint64_t n_triplets,
                         const uint32_t* h1, const uint32_t* h2, const uint32_t* h3, const uint32_t* hit_track_id,
                         uint64_t total_tracks, trax_track_metrics* out);
+/* The same for the context's current CA output, on the device: the tracks
+ * are extracted there, the clone removal runs as independent greedy passes
+ * over the connected components of the "shares a hit" graph (two tracks
+ * without a common hit never compare, so the components' passes give the
+ * list's result), and only the counts come back. */
+int trax_physics_tracks_device(trax_ctx* ctx, uint64_t total_tracks, trax_track_metrics* out);
 
 #ifdef __cplusplus
 }

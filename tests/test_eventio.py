@@ -281,6 +281,7 @@ def test_loaded_events_on_the_gpu_match_the_oracle(eventio, oracle_lib, tmp_path
         ctx.seed_batch(use_graph=True)
         got = ctx.results()
         on_device = physics.triplet_records_device(ctx, fid, fev)
+        tracks_device = physics.track_metrics_device(ctx, fid.size)
     finally:
         ctx.close()
     for k in ("perm", "pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "trip_offsets"):
@@ -293,6 +294,9 @@ def test_loaded_events_on_the_gpu_match_the_oracle(eventio, oracle_lib, tmp_path
     assert a == b
     # the same records counted on the device from the context's triplets
     assert on_device == a
+    # and the track evaluation on the device, against the host's
+    assert tracks_device == physics.track_metrics(got["tracks"], got["track_offsets"], got["trip_h1"],
+                                                  got["trip_h2"], got["trip_h3"], hid, fid.size)
 
 
 @pytest.mark.gpu

@@ -353,6 +353,29 @@ def test_layer_beyond_16bit_grid_counters(ctx, oracle_lib):
     compare(ctx.results(), ref)
 
 
+@pytest.mark.parametrize("config,n_events", [(2, 40), (3, 2)])
+def test_track_evaluation_on_the_device(ctx, config, n_events):
+    """trax_physics_tracks_device (track extraction, clone removal over the
+    components of shared hits, real / fake / distinct tracks on the device)
+    equals the host's list-based evaluation of the same CA output, on ttbar-like
+    events and on the pileup events, where clones share hits densely."""
+    import dataclasses
+    from trax_gb300 import physics
+    if config == 3:
+        batch = events.generate_workload(dataclasses.replace(events.workload(3), n_events=n_events, n_vertices=6))
+    else:
+        batch = events.generate(config, n_events=n_events)
+    ctx.upload(batch)
+    ctx.seed_batch(use_graph=True)
+    got = ctx.results()
+    hid = batch.hit_id[got["perm"]]
+    host = physics.track_metrics(got["tracks"], got["track_offsets"], got["trip_h1"], got["trip_h2"],
+                                 got["trip_h3"], hid, 1000)
+    device = physics.track_metrics_device(ctx, 1000)
+    assert device == host
+    assert host["total"] > 0 and host["filtered"] < host["total"]
+
+
 def test_capacity_overflow_recalibrates(ctx, oracle_lib):
     """A batch of the same shape but far denser hits overflows the capacities
     calibrated on the first: the call recalibrates, recaptures and returns the

@@ -32,7 +32,7 @@ EXPORTED = [
     "trax_get_tracks", "trax_get_grid", "trax_get_hit_perm", "trax_set_block_sizes", "trax_get_launch_config",
     "trax_autotune", "trax_fit_prepare", "trax_fit_forward", "trax_fit_backward", "trax_fit_get_rows",
     "trax_apply_alignment", "trax_events_read", "trax_events_free", "trax_events_raw", "trax_events_load",
-    "trax_events_upload", "trax_physics_triplets_device",
+    "trax_events_upload", "trax_physics_triplets_device", "trax_physics_tracks_device",
     "trax_physics_triplets", "trax_physics_tracks", "trax_geometry_from_files", "trax_host_alloc",
     "trax_host_free",
 ]
@@ -147,6 +147,7 @@ def load() -> ctypes.CDLL:
             "trax_events_upload": ([vp, vp, u64, u64, vp, i32, ctypes.c_float, i32, i32, vp, vp, vp, u64], i32),
             "trax_physics_triplets": ([vp, vp, vp, vp, u32, u32, vp, vp, vp, u64, vp], i32),
             "trax_physics_triplets_device": ([vp, vp, vp, u64, vp], i32),
+            "trax_physics_tracks_device": ([vp, u64, vp], i32),
             "trax_physics_tracks": ([vp, vp, u64, vp, vp, vp, vp, u64, vp], i32),
             "trax_geometry_from_files": ([ctypes.c_char_p, ctypes.c_char_p, u32, vp, vp], i32),
             "trax_host_alloc": ([ctypes.c_size_t], vp),

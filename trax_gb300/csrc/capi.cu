@@ -116,6 +116,10 @@ struct trax_ctx {
   DevBuf raw_x, raw_y, raw_z, raw_layer, raw_det, raw_tid, raw_key, raw_off, raw_scratchOff, raw_scratch;
   // triplet physics counts (trax_physics_triplets_device)
   DevBuf phys_findOff, phys_findIds, phys_flags, phys_counts;
+  // track evaluation (trax_physics_tracks_device)
+  DevBuf trk_isTrack, trk_hitsOf, trk_start, trk_size, trk_real, trk_firstId, trk_parent, trk_compSize,
+      trk_compStart, trk_cursor, trk_members, trk_filtered, trk_hits, trk_entryTrack, trk_owner, trk_table,
+      trk_counts;
   // grid stage
   DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
   // pair stage
@@ -920,7 +924,10 @@ void trax_destroy(trax_ctx* c) {
   DevBuf* bufs[] = {&c->in_x, &c->in_y, &c->in_z, &c->in_layer, &c->in_det, &c->in_hid, &c->in_evt, &c->evOff,
                     &c->layHits, &c->layOff, &c->raw_x, &c->raw_y, &c->raw_z, &c->raw_layer, &c->raw_det,
                     &c->raw_tid, &c->raw_key, &c->raw_off, &c->raw_scratchOff, &c->raw_scratch, &c->phys_findOff,
-                    &c->phys_findIds, &c->phys_flags, &c->phys_counts, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
+                    &c->phys_findIds, &c->phys_flags, &c->phys_counts, &c->trk_isTrack, &c->trk_hitsOf,
+                    &c->trk_start, &c->trk_size, &c->trk_real, &c->trk_firstId, &c->trk_parent, &c->trk_compSize,
+                    &c->trk_compStart, &c->trk_cursor, &c->trk_members, &c->trk_filtered, &c->trk_hits,
+                    &c->trk_entryTrack, &c->trk_owner, &c->trk_table, &c->trk_counts, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
                     &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
@@ -1418,6 +1425,87 @@ int trax_physics_triplets_device(trax_ctx* c, const uint32_t* findable_id, const
   std::vector<uint32_t> clones(S);
   for (size_t k = 0; k < S; ++k) clones[k] = h[S + k] - h[2 * S + k];
   trax::physics_records(E, nLT, offsets.data(), h.data() + 2 * S, h.data(), clones.data(), truthSize.data(), out);
+  return TRAX_OK;
+}
+
+int trax_physics_tracks_device(trax_ctx* c, uint64_t total_tracks, trax_track_metrics* out) {
+  if (!c || !out) return fail(c, TRAX_ERR_ARG, "null argument");
+  if (c->identityHits) return fail(c, TRAX_ERR_STATE, "the hits of caller triplets carry no grid order");
+  *out = trax_track_metrics{0, 0, 0, 0, 0, 0.0, 0.0, 0.0};
+  if (c->stage >= 5 && c->noLinks) return TRAX_OK;  // no links: the reference runs no CA, no tracks
+  if (c->stage < 7) return fail(c, TRAX_ERR_STATE, "cellular automaton not run");
+  const Mode mode = SYNCED;
+  const uint32_t nT = (uint32_t)c->nT;
+  ENSURE(trk_isTrack, (size_t)nT + 1, 4);
+  ENSURE(trk_hitsOf, (size_t)nT + 1, 4);
+  CK(ensure(c, c->scanScratch, scan_scratch_bytes((uint64_t)nT + 1)));
+  uint32_t* isTrack = ptr<uint32_t>(c->trk_isTrack);
+  uint32_t* hitsOf = ptr<uint32_t>(c->trk_hitsOf);
+  const uint32_t* off = ptr<uint32_t>(c->handlers);
+  CK(track_sizes(off, nT, isTrack, hitsOf, c->st));
+  CK(scan_exclusive(isTrack, isTrack, (uint64_t)nT + 1, nullptr, 0, (uint64_t)nT + 1, c->scanScratch.p, dev_err(c),
+                    c->st, nullptr, true));
+  CK(scan_exclusive(hitsOf, hitsOf, (uint64_t)nT + 1, nullptr, 0, (uint64_t)nT + 1, c->scanScratch.p, dev_err(c),
+                    c->st, nullptr, true));
+  uint32_t totals[2];
+  CK(cudaMemcpyAsync(&totals[0], isTrack + nT, 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(&totals[1], hitsOf + nT, 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  RC(check_device_error(c));
+  const uint32_t nTracks = totals[0], nEntries = totals[1];
+  const size_t nk = std::max<size_t>(nTracks, 1) + 1;
+  ENSURE(trk_start, nk, 4); ENSURE(trk_size, nk, 4); ENSURE(trk_real, nk, 4); ENSURE(trk_firstId, nk, 4);
+  ENSURE(trk_parent, nk, 4); ENSURE(trk_compSize, nk, 4); ENSURE(trk_compStart, nk, 4); ENSURE(trk_cursor, nk, 4);
+  ENSURE(trk_members, nk, 4); ENSURE(trk_filtered, nk, 4);
+  ENSURE(trk_hits, std::max<size_t>(nEntries, 1), 4); ENSURE(trk_entryTrack, std::max<size_t>(nEntries, 1), 4);
+  ENSURE(trk_owner, std::max<size_t>(c->nHits, 1), 4);
+  uint32_t tableSize = 1024;
+  while (tableSize < 2ull * nTracks) tableSize <<= 1;
+  ENSURE(trk_table, tableSize, 8);
+  ENSURE(trk_counts, 4, 8);
+  TrackLists t{ptr<uint32_t>(c->trk_start), ptr<uint32_t>(c->trk_size), ptr<uint32_t>(c->trk_real),
+               ptr<uint32_t>(c->trk_firstId), ptr<uint32_t>(c->trk_parent), ptr<uint32_t>(c->trk_compSize),
+               ptr<uint32_t>(c->trk_compStart), ptr<uint32_t>(c->trk_cursor), ptr<uint32_t>(c->trk_members),
+               ptr<uint32_t>(c->trk_filtered), ptr<uint32_t>(c->trk_hits), ptr<uint32_t>(c->trk_entryTrack),
+               ptr<uint32_t>(c->trk_owner)};
+  CK(cudaMemsetAsync(t.owner, 0xFF, std::max<size_t>(c->nHits, 1) * 4, c->st));
+  CK(cudaMemsetAsync(t.compSize, 0, nk * 4, c->st));
+  CK(cudaMemsetAsync(t.cursor, 0, nk * 4, c->st));
+  CK(cudaMemsetAsync(c->trk_table.p, 0, (size_t)tableSize * 8, c->st));
+  CK(cudaMemsetAsync(c->trk_counts.p, 0, 4 * 8, c->st));
+  CK(track_extract(off, ptr<uint32_t>(c->tracks), nT, ptr<uint32_t>(c->h1), ptr<uint32_t>(c->h2),
+                   ptr<uint32_t>(c->h3), ptr<uint32_t>(c->phid), isTrack, hitsOf, t, c->st));
+  // components of the "shares a hit" graph: union-find rounds until stable
+  uint32_t* changed = ptr<uint32_t>(c->trk_counts) + 6;  // a spare word of the counts buffer
+  bool stable = false;
+  for (int round = 0; round < 64 && !stable; ++round) {
+    CK(cudaMemsetAsync(changed, 0, 4, c->st));
+    CK(track_union_step(t, nTracks, nEntries, changed, c->st));
+    uint32_t h = 0;
+    CK(cudaMemcpyAsync(&h, changed, 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    stable = h == 0;
+  }
+  if (!stable) return fail(c, TRAX_ERR_TIMEOUT, "track components did not settle in 64 rounds");
+  CK(track_members(t, nTracks, false, c->st));
+  CK(scan_exclusive(t.compSize, t.compStart, (uint64_t)nTracks + 1, nullptr, 0, (uint64_t)nTracks + 1,
+                    c->scanScratch.p, dev_err(c), c->st, nullptr, true));
+  CK(track_members(t, nTracks, true, c->st));
+  unsigned long long* counts = ptr<unsigned long long>(c->trk_counts);
+  CK(track_greedy(t, nTracks, ptr<unsigned long long>(c->trk_table), tableSize - 1, counts, c->st));
+  unsigned long long h[3];
+  CK(cudaMemcpyAsync(h, counts, 3 * 8, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  RC(check_device_error(c));
+  out->total = nTracks;
+  out->filtered = h[0];
+  out->valid = h[1];
+  out->valid_unique = h[2];
+  out->fakes = h[0] - h[1];
+  const double nf = (double)h[0];
+  out->fake_rate = nf > 0 ? (double)out->fakes / nf : 0.0;
+  out->clone_rate = nf > 0 ? (double)(h[1] - h[2]) / nf : 0.0;
+  out->efficiency = total_tracks ? (double)h[2] / (double)total_tracks : 0.0;
   return TRAX_OK;
 }
 

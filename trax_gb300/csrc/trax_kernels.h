@@ -66,6 +66,43 @@ cudaError_t physics_counts(const uint32_t* h1, const uint32_t* h2, const uint32_
                            const uint32_t* findIds, uint32_t* fakes, uint32_t* realFindable, uint32_t* foundFlags,
                            uint32_t* found, cudaStream_t st, uint32_t* launches);
 
+// ------------------------------------------------------ track evaluation
+// The tracks of the CA output (k_tracks.cu): [nTracks] hit-list start and
+// size, real flag, first hit's simulated track id, union-find parent,
+// component size / start / cursor (nTracks + 1 for the scan), members and
+// the filtered list per component; [entries] hits and their track; [hits]
+// the smallest track holding each hit.
+struct TrackLists {
+  uint32_t* start;
+  uint32_t* size;
+  uint32_t* real;
+  uint32_t* firstId;
+  uint32_t* parent;
+  uint32_t* compSize;
+  uint32_t* compStart;
+  uint32_t* cursor;
+  uint32_t* members;
+  uint32_t* filtered;
+  uint32_t* hits;
+  uint32_t* entryTrack;
+  uint32_t* owner;
+};
+// isTrack[i], hitsOf[i] for i <= nT (the +1 slots zero): chains of three or
+// more triplets and their hit counts
+cudaError_t track_sizes(const uint32_t* off, uint32_t nT, uint32_t* isTrack, uint32_t* hitsOf, cudaStream_t st);
+// with isTrack / hitsOf scanned into trackOf / hitStart
+cudaError_t track_extract(const uint32_t* off, const uint32_t* chain, uint32_t nT, const uint32_t* h1,
+                          const uint32_t* h2, const uint32_t* h3, const uint32_t* hitTrack, const uint32_t* trackOf,
+                          const uint32_t* hitStart, TrackLists t, cudaStream_t st);
+// one union-find round (hook, compress); *changed set when a root moved
+cudaError_t track_union_step(TrackLists t, uint32_t nTracks, uint32_t nEntries, uint32_t* changed, cudaStream_t st);
+// place == false: component sizes; true: members at the scanned starts
+cudaError_t track_members(TrackLists t, uint32_t nTracks, bool place, cudaStream_t st);
+// per component the greedy clone removal; counts[0..2]: filtered, real,
+// distinct real simulated track ids (table: 2^k zeroed slots, mask 2^k - 1)
+cudaError_t track_greedy(TrackLists t, uint32_t nTracks, unsigned long long* table, uint32_t tableMask,
+                         unsigned long long* counts, cudaStream_t st);
+
 // ------------------------------------------------------------ grid build
 struct GridInput {
   const float* x;

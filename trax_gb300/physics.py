@@ -73,3 +73,11 @@ def track_metrics(tracks, track_offsets, h1, h2, h3, hit_track_id, total_tracks:
     if rc != capi.TRAX_OK:
         raise capi.TraxError(rc, "trax_physics_tracks failed")
     return {f[0]: getattr(out, f[0]) for f in TrackMetricsC._fields_}
+
+
+def track_metrics_device(ctx: "capi.Context", total_tracks: int) -> Dict[str, float]:
+    """track_metrics for the context's current CA output, evaluated on the device
+    (trax_physics_tracks_device)."""
+    out = TrackMetricsC()
+    ctx._check(ctx._L.trax_physics_tracks_device(ctx._h, total_tracks, ctypes.byref(out)))
+    return {f[0]: getattr(out, f[0]) for f in TrackMetricsC._fields_}
