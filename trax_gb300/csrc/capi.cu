@@ -125,7 +125,7 @@ struct trax_ctx {
   // pair stage
   DevBuf segOuter, taskBase, taskCount, taskOrdered, pairs, pairOffsets;
   // prediction / filter
-  DevBuf candCount, predWarps, predKeep, cands, candOffsets, flagWords, flagSums, h1, h2, h3, tripOffsets;
+  DevBuf candLocal, predWarps, predKeep, cands, candOffsets, flagWords, flagSums, h1, h2, h3, tripOffsets;
   // connectivity / fit / CA
   DevBuf eta, segOf, segStart, linkCount, linkRun, cflags, basis, follower, connS, nonConnS, connW, nonConnW, connIdx, nonConnIdx, pt;
   DevBuf states, inStart, inCursor, inList, best, isBest, handlers, tracks;
@@ -454,15 +454,17 @@ int stage_predict(trax_ctx* c, Mode mode) {
   const uint32_t* nPairsDev = slot(c, S_PAIRS);
   const uint64_t maxPairs = mode == SYNCED ? c->nPairs : c->capPairs;
   const uint64_t maxWarps = (maxPairs + 31) / 32;
-  ENSURE(candCount, maxPairs + 1, 4);
+  // per pair the offset of its candidates within its warp of 32 pairs, per
+  // warp the candidates' sum (scanned into the warp's first position)
+  ENSURE(candLocal, maxPairs + 1, 4);
   ENSURE(predWarps, maxWarps + 1, 4);
   ENSURE(predKeep, maxPairs * TRAX_PRED_KEEP, 4);
   ENSURE(candOffsets, S + 1, 4);
-  uint32_t* candCount = ptr<uint32_t>(c->candCount);
+  uint32_t* candLocal = ptr<uint32_t>(c->candLocal);
   uint32_t* warpSums = ptr<uint32_t>(c->predWarps);
   KBEG(TK_PRED_COUNT);
   CK(predict_pairs(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
-                   candCount, warpSums, slot(c, S_PRED_WARPS), ptr<uint32_t>(c->predKeep), nullptr, 0,
+                   candLocal, warpSums, slot(c, S_PRED_WARPS), ptr<uint32_t>(c->predKeep), nullptr, 0,
                    slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
   KEND(TK_PRED_COUNT);
   // the prefix sum runs over the per-warp sums of the counts
@@ -476,10 +478,10 @@ int stage_predict(trax_ctx* c, Mode mode) {
   ENSURE(cands, maxCands, 8);
   KBEG(TK_PRED_EMIT);
   CK(predict_pairs(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
-                   candCount, warpSums, nullptr, ptr<uint32_t>(c->predKeep), ptr<uint2>(c->cands), maxCands,
+                   candLocal, warpSums, nullptr, ptr<uint32_t>(c->predKeep), ptr<uint2>(c->cands), maxCands,
                    slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
   KEND(TK_PRED_EMIT);
-  CK(predict_offsets(c->cfg, ptr<uint32_t>(c->pairOffsets), nPairsDev, candCount, warpSums,
+  CK(predict_offsets(c->cfg, ptr<uint32_t>(c->pairOffsets), nPairsDev, candLocal, warpSums,
                      ptr<uint32_t>(c->candOffsets), c->st, &c->launches));
   return TRAX_OK;
 }
@@ -724,7 +726,7 @@ int size_device_buffers(trax_ctx* c) {
   ENSURE(taskCount, c->capTasks + 1, 4);
   ENSURE(taskOrdered, c->capTasks + 1, 1);
   ENSURE(pairs, c->capPairs, 8);
-  ENSURE(candCount, c->capPairs + 1, 4);
+  ENSURE(candLocal, c->capPairs + 1, 4);
   ENSURE(predWarps, (c->capPairs + 31) / 32 + 1, 4);
   ENSURE(predKeep, c->capPairs * TRAX_PRED_KEEP, 4);
   ENSURE(cands, c->capCands, 8);
@@ -929,7 +931,7 @@ void trax_destroy(trax_ctx* c) {
                     &c->trk_compStart, &c->trk_cursor, &c->trk_members, &c->trk_filtered, &c->trk_hits,
                     &c->trk_entryTrack, &c->trk_owner, &c->trk_table, &c->trk_counts, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
-                    &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candCount, &c->predWarps, &c->predKeep, &c->cands,
+                    &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candLocal, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->linkRun, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS, &c->connW, &c->nonConnW,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,
