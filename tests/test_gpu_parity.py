@@ -175,6 +175,19 @@ def test_empty_layers_and_events(ctx, oracle_lib):
     compare(ctx.results(), ref)
 
 
+def test_degenerate_hits_match_oracle(ctx, oracle_lib):
+    """Hits on the edge cases of the window arithmetic (radius 0 from
+    sign(0), phi = +-pi, the y axis, 0/0 TIP, duplicates, row boundaries,
+    denormal and 1e-20 coordinates): stage by stage and in one graph replay."""
+    from tests.test_oracle_kats import degenerate_batch
+    b = degenerate_batch()
+    ref = oracle_lib.run(b)[0]
+    compare(stagewise(ctx, b), ref)
+    ctx.upload(b)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+
+
 def test_single_event_single_track(ctx, oracle_lib):
     batch = events.generate(0, n_events=1)
     ref = oracle_lib.run(batch)[0]

@@ -207,3 +207,60 @@ def test_config0_finds_most_muons(oracle_lib):
     findable = {(int(e), int(t)) for e, t in set(zip(b.event.tolist(), b.hit_id.tolist())) if t
                 and len({int(l) for l in lay[(b.event == e) & (b.hit_id == t)]}) == 3}
     assert len(found & findable) >= 0.9 * len(findable)
+
+
+def degenerate_batch():
+    """Two config-1 events with hits moved onto the edge cases of the
+    reference's window arithmetic: outer hits on the x axis (sign(y) = 0 gives
+    radius 0 and NaN/inf windows, PairGeneratorBeamspot.h:111-112), phi = +pi
+    and -pi exactly (the overflow phi column, TripletThetaPhiPredictor.h:193),
+    the y axis, an outer hit at the inner hit's transverse point (0/0 in the
+    prediction's TIP), a duplicated third-layer hit, z on the first row and on
+    a row boundary, a denormal y, and outer radii of 1e-20 and 1e-3."""
+    b = events.generate(1, n_events=2)
+    x, y, z = b.x.copy(), b.y.copy(), b.z.copy()
+    f = np.float32
+
+    def idx(e, l, k):
+        return int(np.nonzero((b.event == e) & (b.layer == l))[0][k])
+
+    def rad(i):
+        return f(np.hypot(x[i], y[i]))
+
+    sz = f(f(300) - f(-300)) / f(b.n_z)
+    for e in (0, 1):
+        i = idx(e, 2, 0); x[i], y[i] = rad(i), f(0.0)
+        i = idx(e, 2, 1); x[i], y[i] = -rad(i), f(-0.0)
+        for l in (1, 3):
+            i = idx(e, l, 2); x[i], y[i] = -rad(i), f(0.0)
+            i = idx(e, l, 3); x[i], y[i] = f(0.0), rad(i)
+        i, j = idx(e, 2, 4), idx(e, 1, 4); x[i], y[i] = x[j], y[j]
+        i, j = idx(e, 3, 5), idx(e, 3, 6); x[i], y[i], z[i] = x[j], y[j], z[j]
+        i = idx(e, 1, 7); z[i] = f(-300.0)
+        for k, l in ((8, 1), (9, 2), (10, 3)):
+            i = idx(e, l, k); z[i] = f(-300.0) + f(b.n_z // 2) * sz
+        i = idx(e, 1, 11); x[i], y[i] = -rad(i), f(-1e-30)
+        i = idx(e, 2, 6); x[i], y[i] = f(1e-20), f(1e-20)
+        i = idx(e, 2, 7); x[i], y[i] = f(1e-3), f(-1e-3)
+    cols = {k: getattr(b, k) for k in ("layer", "det_id", "hit_id", "event")}
+    cols.update(x=x, y=y, z=z)
+    return events._assemble(cols, b.layer_hits, b)
+
+
+def test_oracle_on_degenerate_hits(oracle_lib):
+    b = degenerate_batch()
+    r = oracle_lib.run(b)[0]
+    # phi = +pi lands in the overflow column nP, which the prediction's row
+    # end includes and the pair window's does not (Q8)
+    f = np.float32
+    sp = (f(np.pi) - f(-np.pi)) / f(b.n_phi)
+    phi = np.arctan2(f(0.0), -np.hypot(b.x[:1], b.y[:1]).astype(np.float32))[0]
+    assert phi == f(np.pi) and np.floor((phi - f(-np.pi)) / sp) == b.n_phi
+    C = (b.n_z + 1) * (b.n_phi + 1)
+    grid = r["grid"].reshape(b.n_events, b.n_layers, C).astype(np.int64)
+    ends = np.concatenate([grid[..., 1:], grid[..., -1:]], axis=-1)
+    overflow = (ends - grid).reshape(b.n_events, b.n_layers, b.n_z + 1, b.n_phi + 1)[..., b.n_phi]
+    assert overflow[:, 0].sum() >= 2 and overflow[:, 2].sum() >= 2
+    # every hit is placed once and the chain runs to the tracks
+    assert np.array_equal(np.sort(r["perm"]), np.arange(b.n_hits))
+    assert r["stats_dict"]["triplets"] > 0 and r["stats_dict"]["links"] > 0
