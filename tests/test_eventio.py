@@ -4,7 +4,10 @@ protobuf encoder is read back field by field; the loader is compared with a
 plain-Python restatement of HitCollection::addEvent (HitCollection.cpp:21-180);
 the physics records with hand-counted cases; and, where the reference's
 ttbar fixture is present (this container only), its 10 events run through
-the oracle chain against the reference's published physics numbers, loosely."""
+the oracle chain against the reference's published physics numbers, loosely.
+The same 10 events, as the loader hands them to the seeding chain, are kept
+in tests/golden/ttbar10_loaded.npz (made by tests/golden/make_ttbar_fixture.py)
+and run through the oracle here and the GPU chain on the GPU machine."""
 import os
 import struct
 
@@ -15,6 +18,24 @@ from trax_gb300 import events
 
 REF = "/root/reference"
 TTBAR = os.path.join(REF, "plotting/data/physics/hits.ttBar.pb")
+GOLDEN_TTBAR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ttbar10_loaded.npz")
+
+
+def ttbar_fixture():
+    """(EventBatch, findable ids, findable events, the fixture's arrays): the
+    reference's 10 ttbar events at its ttBar.reco.conf settings, loaded."""
+    import dataclasses
+    d = np.load(GOLDEN_TTBAR)
+    fields = dataclasses.fields(events.LayerTriplet)
+    lts = [events.LayerTriplet(*[int(v) if f.type in ("int", int) else float(v) for f, v in zip(fields, row)])
+           for row in d["lts"]]
+    proto = events.EventBatch(x=None, y=None, z=None, layer=None, det_id=None, hit_id=None, event=None,
+                              event_offsets=None, layer_hits=None, layer_offsets=None, min_r=d["min_r"],
+                              max_r=d["max_r"], lts=lts, n_z=50, n_phi=8, min_pt=1.0, d_eta_cut=events.D_ETA_CUT)
+    cols = {k: d[k].astype(np.float32 if k in "xyz" else np.uint32)
+            for k in ("x", "y", "z", "layer", "det_id", "hit_id", "event")}
+    batch = events._assemble(cols, d["layer_hits"], proto)
+    return batch, d["findable_id"], d["findable_event"], d
 
 
 # ---------------------------------------------------------------- encoder
@@ -257,6 +278,61 @@ def test_reference_ttbar_fixture(eventio, oracle_lib):
     assert 0.7 <= recs[0]["efficiency"] <= 0.9
     assert 0.5 <= recs[-1]["efficiency"] <= 0.9
     assert recs[-1]["fake_rate"] <= 0.6 and recs[-1]["clone_rate"] <= 0.2
+
+
+def test_ttbar_fixture_through_the_oracle(eventio, oracle_lib):
+    """The committed ttbar fixture gives the oracle's triplets and physics
+    stored beside it; where the reference is present, the fixture is what
+    the loader makes of its file."""
+    from trax_gb300 import physics
+    batch, fid, fev, d = ttbar_fixture()
+    r = oracle_lib.run(batch)[0]
+    assert r["stats_dict"]["triplets"] == int(d["oracle_triplets"])
+    recs = physics.triplet_records(r["trip_h1"], r["trip_h2"], r["trip_h3"], r["trip_offsets"], batch.n_events,
+                                   len(batch.lts), batch.hit_id[r["perm"]], fid, fev)
+    assert [q["efficiency"] for q in recs] == d["oracle_efficiency"].tolist()
+    assert [q["fake_rate"] for q in recs] == d["oracle_fake_rate"].tolist()
+    if os.path.exists(TTBAR):
+        from tests.golden.make_ttbar_fixture import ttbar_layer_triplets
+        mn, mx = eventio.geometry_from_files(os.path.join(REF, "configs/radiusDictionary.dat"),
+                                             os.path.join(REF, "configs/detectorRadius.dat"), 13)
+        b2, fid2, fev2 = eventio.EventFile(TTBAR).load(ttbar_layer_triplets(), 1.0, only_tracks=True, n_z=50,
+                                                       n_phi=8, min_r=mn[:8], max_r=mx[:8])
+        for k in ("x", "y", "z", "layer", "det_id", "hit_id", "event", "layer_hits"):
+            assert np.array_equal(getattr(b2, k), getattr(batch, k)), k
+        assert np.array_equal(fid2, fid) and np.array_equal(fev2, fev)
+
+
+@pytest.mark.gpu
+def test_reference_ttbar_events_on_the_gpu(oracle_lib):
+    """The reference's own 10 ttbar events (the committed fixture) through the
+    GPU chain: every stage equal to the oracle, and the physics records and
+    track evaluation counted on the device equal to the host's and to the
+    values stored with the fixture."""
+    from trax_gb300 import capi, physics
+    batch, fid, fev, d = ttbar_fixture()
+    ref = oracle_lib.run(batch)[0]
+    ctx = capi.Context(0)
+    try:
+        ctx.upload(batch)
+        ctx.seed_batch(use_graph=True)
+        got = ctx.results()
+        on_device = physics.triplet_records_device(ctx, fid, fev)
+        tracks_device = physics.track_metrics_device(ctx, fid.size)
+    finally:
+        ctx.close()
+    for k in ("perm", "grid", "pairs", "pair_offsets", "cands", "cand_offsets", "trip_h1", "trip_h2", "trip_h3",
+              "trip_offsets", "link_basis", "link_follower", "ca_states", "tracks", "track_offsets"):
+        assert np.array_equal(np.asarray(got[k]), np.asarray(ref[k])), k
+    for k in ("eta", "pt"):
+        assert np.array_equal(np.asarray(got[k]).view(np.uint32), np.asarray(ref[k]).view(np.uint32)), k
+    hid = batch.hit_id[got["perm"]]
+    host = physics.triplet_records(got["trip_h1"], got["trip_h2"], got["trip_h3"], got["trip_offsets"],
+                                   batch.n_events, len(batch.lts), hid, fid, fev)
+    assert on_device == host
+    assert [q["efficiency"] for q in host] == d["oracle_efficiency"].tolist()
+    assert tracks_device == physics.track_metrics(got["tracks"], got["track_offsets"], got["trip_h1"],
+                                                  got["trip_h2"], got["trip_h3"], hid, fid.size)
 
 
 @pytest.mark.gpu
