@@ -97,6 +97,8 @@ def lib():
                                            ctypes.c_void_p, ctypes.c_uint64]
             L.oracle_min_radius_curvature.argtypes = [ctypes.c_float]
             L.oracle_min_radius_curvature.restype = ctypes.c_float
+            L.oracle_dphi_check.argtypes = [ctypes.c_uint64] + [ctypes.c_void_p] * 7
+            L.oracle_dphi_check.restype = None
             _lib = L
         return _lib
 
@@ -229,6 +231,15 @@ def math_eval(fn: str, a: np.ndarray, b: Optional[np.ndarray] = None) -> np.ndar
     out = np.zeros_like(a)
     lib().oracle_math_eval(code, _ptr(a), _ptr(b), _ptr(out), a.size)
     return out
+
+
+def dphi_check(ux, uy, vx, vy, cut):
+    """(atan2 evaluation of the dphi cut, the kernels' cross/dot decision: 1, 0 or -1 undecided)."""
+    cols = [np.ascontiguousarray(a, dtype=np.float32) for a in (ux, uy, vx, vy, cut)]
+    n = cols[0].size
+    exact, decided = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    lib().oracle_dphi_check(n, *[_ptr(a) for a in cols], _ptr(exact), _ptr(decided))
+    return exact, decided
 
 
 def min_radius_curvature(min_pt: float) -> float:

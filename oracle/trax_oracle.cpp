@@ -1162,4 +1162,20 @@ void oracle_math_eval(int fn, const float* a, const float* b, float* out, uint64
 
 float oracle_min_radius_curvature(float min_pt) { return min_radius_curvature(min_pt); }
 
+// The dphi cut of transverse segment pairs (u, v): filterCount's atan2
+// evaluation (TripletThetaPhiFilter.h:118-128, as in filter_one) and the
+// kernels' cross/dot decision trax::dphi_decide, for the tests that check
+// the decision never disagrees with the evaluation.
+void oracle_dphi_check(uint64_t n, const float* ux, const float* uy, const float* vx, const float* vy,
+                       const float* cut, int32_t* exact, int32_t* decided) {
+  for (uint64_t i = 0; i < n; ++i) {
+    float delta = atan2_(vy[i], vx[i]) - atan2_(uy[i], ux[i]);
+    delta += (delta > M_PI_F) ? -2 * M_PI_F : (delta < -M_PI_F) ? 2 * M_PI_F : 0;
+    exact[i] = fabs_(delta) <= cut[i] ? 1 : 0;
+    float lo, hi;
+    trax::dphi_tan_bounds(cut[i], lo, hi);
+    decided[i] = trax::dphi_decide(lo, hi, ux[i], uy[i], vx[i], vy[i]);
+  }
+}
+
 }  // extern "C"

@@ -94,6 +94,8 @@ void oracle_prefix_sum_blelloch(uint32_t* data, uint32_t n, uint32_t wg);
 // Element-wise evaluation of the shared math (trax_math.h):
 // fn 0 atan2(a, b), 1 acos(a), 2 atan(a), 3 asinh(a), 4 log(a).
 void oracle_math_eval(int fn, const float* a, const float* b, float* out, uint64_t n);
+void oracle_dphi_check(uint64_t n, const float* ux, const float* uy, const float* vx, const float* vy,
+                       const float* cut, int32_t* exact, int32_t* decided);
 
 // minRadiusCurvature(minPt) of TripletConfiguration.cpp:36-43 with IDEAL_BZ.
 float oracle_min_radius_curvature(float min_pt);

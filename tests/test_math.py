@@ -83,3 +83,36 @@ def test_min_radius_curvature(oracle_lib):
     # TripletConfiguration.cpp:36-43: 87.52 cm at 1 GeV, 61.27 cm at 0.7 GeV (IDEAL_BZ = 3.8112 T)
     assert abs(oracle_lib.min_radius_curvature(1.0) - 87.52) < 0.01
     assert abs(oracle_lib.min_radius_curvature(0.7) - 61.27) < 0.01
+
+
+def test_dphi_decision_never_disagrees_with_atan2(oracle_lib, rng):
+    """The filter kernel decides the dphi cut from the cross and dot products
+    of the two transverse segments wherever that is certain; it must never
+    contradict the atan2 evaluation of filterCount
+    (TripletThetaPhiFilter.h:118-128), and away from the cut it must decide."""
+    f32 = np.float32
+    n = 1_000_000
+    cuts = rng.choice(np.array([0.0, 0.01, 0.075, 0.2, 0.4, 1.0], f32), n)
+    lu, lv = 10.0 ** rng.uniform(-2, 2.5, n), 10.0 ** rng.uniform(-2, 2.5, n)
+    a = rng.uniform(-np.pi, np.pi, n)
+    near = rng.random(n) < 0.6
+    d = np.where(near, cuts.astype(np.float64) + rng.uniform(-3e-4, 3e-4, n), rng.uniform(0, np.pi, n))
+    d *= rng.choice([-1.0, 1.0], n)
+    ox, oy = rng.uniform(-60, 60, (2, n))  # hit coordinates, then the segments as the kernel forms them
+    ax, ay = ox.astype(f32), oy.astype(f32)
+    bx, by = (ox + lu * np.cos(a)).astype(f32), (oy + lu * np.sin(a)).astype(f32)
+    cx, cy = (bx + lv * np.cos(a + d)).astype(f32), (by + lv * np.sin(a + d)).astype(f32)
+    ux, uy, vx, vy = bx - ax, by - ay, cx - bx, cy - by
+    exact, dec = oracle_lib.dphi_check(ux, uy, vx, vy, cuts)
+    assert np.all((dec == -1) | (dec == exact))
+    ang = np.abs(np.angle((vx + 1j * vy).astype(np.complex128) / (ux + 1j * uy).astype(np.complex128)))
+    far = np.abs(ang - cuts) > 2e-4
+    assert np.mean(dec[far] == -1) < 1e-4
+    assert np.mean(dec[~far] == -1) > 0.3  # the band around the cut goes to atan2
+    # degenerate segments and cuts: undecided or equal
+    specials = np.array([0.0, -0.0, 1e-20, -1e-20, 1e-38, 1.0, -1.0, 1e20, np.inf, -np.inf, np.nan], f32)
+    g = np.stack(np.meshgrid(specials, specials, specials, specials, indexing="ij"), 0).reshape(4, -1)
+    for cut in (0.075, 0.0, -0.1, 1.5, np.nan, np.inf):
+        c = np.full(g.shape[1], cut, f32)
+        exact, dec = oracle_lib.dphi_check(g[0], g[1], g[2], g[3], c)
+        assert np.all((dec == -1) | (dec == exact)), cut

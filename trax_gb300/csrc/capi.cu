@@ -299,6 +299,7 @@ int build_config(trax_ctx* c, bool seeding = true) {
     g.dThetaCut[p] = t.dtheta_cut;
     g.sigmaZ[p] = t.sigma_z;
     g.dPhiCut[p] = t.dphi_cut;
+    dphi_tan_bounds(t.dphi_cut, g.dPhiTanLo[p], g.dPhiTanHi[p]);
     g.sigmaPhi[p] = t.sigma_phi;
     g.tipCut[p] = t.tip_cut;
     g.z0[p] = t.z0;

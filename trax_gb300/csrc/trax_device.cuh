@@ -29,6 +29,7 @@ struct DevConfig {
   float dThetaCut[TRAX_MAX_LT], sigmaZ[TRAX_MAX_LT], dPhiCut[TRAX_MAX_LT];
   float sigmaPhi[TRAX_MAX_LT], tipCut[TRAX_MAX_LT], z0[TRAX_MAX_LT];
   float pairSigmaPhi[TRAX_MAX_LT];  // pairSpreadPhi bit pattern read as float
+  float dPhiTanLo[TRAX_MAX_LT], dPhiTanHi[TRAX_MAX_LT];  // dphi_tan_bounds of dPhiCut
   float minR[TRAX_MAX_LAYERS], maxR[TRAX_MAX_LAYERS];
   // acos(r / (2 minRadiusCurvature)) of each layer's min/max radius, computed on
   // the host with the same trax_math.h code as the kernels would

@@ -38,6 +38,8 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <cmath>
+
 #include "trax_math_coeffs.h"
 
 #if defined(__CUDACC__)
@@ -344,6 +346,50 @@ TRAX_HD void normalize2(float& vx, float& vy) {
   float l = sqrt_(vx * vx + vy * vy);
   vx = div_(vx, l);
   vy = div_(vy, l);
+}
+
+// ------------------------------------------- the dphi cut away from its edge
+// The filter's dphi cut (TripletThetaPhiFilter.h:118-128) compares the
+// wrapped difference of atan2(v) and atan2(u), u = B - A and v = C - B in the
+// transverse plane, with dPhiCut.  Away from the cut the answer follows from
+// the cross and dot products of u and v alone:
+// - the evaluated difference is within 2.1e-6 rad of the true angle between
+//   u and v: atan2_ is within 3 ulp of each direction (7.2e-7 rad below pi),
+//   the subtraction and the +-2 pi_f wrap round by 2.4e-7 rad each, and
+//   pi_f is 8.7e-8 from pi;
+// - the FP32 cross and dot products, a difference and a sum of two rounded
+//   products, are within 2^-23 |u| |v| of the exact ones, which for angles up
+//   to 1 rad puts the angle they give within 6e-7 rad of the true one, as
+//   long as |u| |v| stays far from the under- and overflow limits.
+// With a margin of TRAX_DPHI_MARGIN rad on both sides of the cut,
+// cross <= dot tan(cut - margin) means the cut passes and
+// cross >= dot tan(cut + margin) means it fails.  Candidates in between,
+// degenerate or non-finite vectors, and cuts outside [0, 1] rad (whose
+// tanHi is infinite) are left to the atan2 evaluation.
+// Returns 1 (passes), 0 (fails) or -1 (undecided).
+#define TRAX_DPHI_MARGIN 1e-4
+
+TRAX_HD int dphi_decide(float tanLo, float tanHi, float ux, float uy, float vx, float vy) {
+  if (!(tanHi < bits2f(0x7f800000u))) return -1;
+  const float nm = (fabs_(ux) + fabs_(uy)) * (fabs_(vx) + fabs_(vy));
+  if (!(nm >= 1e-30f && nm <= 1e30f)) return -1;
+  const float cr = fabs_(ux * vy - uy * vx), dt = ux * vx + uy * vy;
+  if (dt <= 0.0f) return 0;  // at least pi/2 - 6e-7 rad apart
+  if (cr <= dt * tanLo) return 1;
+  if (cr >= dt * tanHi) return 0;
+  return -1;
+}
+
+// tan(cut -+ margin) of a dphi cut, or (-1, inf) for a cut outside [0, 1] rad
+// (host side; the kernels read the pair from the configuration)
+inline void dphi_tan_bounds(float cut, float& tanLo, float& tanHi) {
+  if (cut >= 0.0f && cut <= 1.0f) {
+    tanLo = (float)std::tan((double)cut - TRAX_DPHI_MARGIN);
+    tanHi = (float)std::tan((double)cut + TRAX_DPHI_MARGIN);
+  } else {
+    tanLo = -1.0f;
+    tanHi = bits2f(0x7f800000u);
+  }
 }
 
 }  // namespace trax

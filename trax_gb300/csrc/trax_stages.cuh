@@ -132,6 +132,13 @@ __device__ __forceinline__ bool filter_dphi(float dPhiCut, float4 A, float4 B, f
   return fabs_(delta) <= dPhiCut;
 }
 
+// The dphi part decided from cross and dot products where that is certain
+// (dphi_decide), else by the atan2 evaluation above.
+__device__ __forceinline__ bool filter_dphi_fast(const DevConfig& cfg, uint32_t lt, float4 A, float4 B, float4 Cc) {
+  const int q = dphi_decide(cfg.dPhiTanLo[lt], cfg.dPhiTanHi[lt], B.x - A.x, B.y - A.y, Cc.x - B.x, Cc.y - B.y);
+  return q > 0 || (q < 0 && filter_dphi(cfg.dPhiCut[lt], A, B, Cc));
+}
+
 // The dtheta, TIP and curvature parts (:84-117, :130-154).
 __device__ __forceinline__ bool filter_rest(const DevConfig& cfg, uint32_t lt, float4 A, float4 B, float4 Cc) {
   bool valid = true;
