@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--plain-events", type=int, default=48)
     p.add_argument("--cpu-sample", type=int, default=128)
     p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-pipe-steps", type=int, default=25,
+                   help="steps per context of the pipelined end-to-end run (enough to amortise its fill and drain)")
     p.add_argument("--e2e-contexts", type=int, default=4,
                    help="contexts (each with its own stream and host thread) that overlap copies with kernels")
     p.add_argument("--no-plain", action="store_true")
@@ -474,7 +476,7 @@ def run_ours(args, ranks):
                      capi.pinned_empty((max(st.n_track_entries, 1),), np.uint32),
                      capi.pinned_empty((st.n_triplets + 1,), np.uint32)])
             pipes.append((c2, outs))
-        steps_each = max(args.e2e_steps, 2)
+        steps_each = max(args.e2e_pipe_steps, 2)
         errors = []
 
         def worker(c2, outs):
