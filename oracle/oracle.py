@@ -10,7 +10,7 @@ import ctypes
 import os
 import subprocess
 import threading
-from typing import Dict, List, Optional
+from typing import Dict, List, Optional, Sequence
 
 import numpy as np
 
@@ -111,8 +111,10 @@ class OracleError(RuntimeError):
     pass
 
 
-def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1) -> List[Dict[str, np.ndarray]]:
-    """Run the oracle over an EventBatch; one dict of arrays per event group."""
+def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1,
+        arrays: Optional[Sequence[str]] = None) -> List[Dict[str, np.ndarray]]:
+    """Run the oracle over an EventBatch; one dict of arrays per event group (only
+    `arrays` and the stats when given, e.g. ("stats",) for timing runs)."""
     L = lib()
     keep = []
 
@@ -158,7 +160,7 @@ def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1) 
         out = []
         for g in range(L.oracle_n_groups(h)):
             d = {}
-            for name in ARRAYS:
+            for name in (ARRAYS if arrays is None else [a for a in ARRAYS if a in arrays or a == "stats"]):
                 n = L.oracle_size(h, g, name.encode())
                 if n < 0:
                     continue
