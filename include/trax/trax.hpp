@@ -130,8 +130,11 @@ class TripletConfigurations {
   // with the reference's ideal field and constants
   float minRadiusCurvature() const { return minRadiusCurvature(minPt_); }
   static float minRadiusCurvature(float minPt) {
+    // the double IDEAL_BZ goes through the float Bz parameter of
+    // minRadiusCurvature(minPt, Bz) (TripletConfiguration.h:56-70)
     const double IDEAL_BZ = 3.8112, Q = 1.602177E-19, GEV_C = 5.344286E-19;
-    return (float)(minPt * GEV_C / (IDEAL_BZ * Q) * 1E2);
+    const float Bz = (float)IDEAL_BZ;
+    return (float)(minPt * GEV_C / (Bz * Q) * 1E2);
   }
 
   // loadTripletConfigurationFromFile (TripletConfiguration.cpp:70-107): the

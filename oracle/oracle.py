@@ -111,11 +111,9 @@ class OracleError(RuntimeError):
     pass
 
 
-def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1,
-        arrays: Optional[Sequence[str]] = None) -> List[Dict[str, np.ndarray]]:
-    """Run the oracle over an EventBatch; one dict of arrays per event group (only
-    `arrays` and the stats when given, e.g. ("stats",) for timing runs)."""
-    L = lib()
+def make_input(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1):
+    """The oracle_input struct for an EventBatch, and the arrays it points into
+    (keep them alive while the struct is used)."""
     keep = []
 
     def arr(a, dt):
@@ -152,6 +150,15 @@ def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1,
     inp.min_r, inp.max_r = arr(batch.min_r, np.float32), arr(batch.max_r, np.float32)
     inp.d_eta_cut = batch.d_eta_cut
     inp.n_threads, inp.event_grouping, inp.n_workers = n_threads, event_grouping, n_workers
+    return inp, keep
+
+
+def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1,
+        arrays: Optional[Sequence[str]] = None) -> List[Dict[str, np.ndarray]]:
+    """Run the oracle over an EventBatch; one dict of arrays per event group (only
+    `arrays` and the stats when given, e.g. ("stats",) for timing runs)."""
+    L = lib()
+    inp, keep = make_input(batch, n_threads, event_grouping, n_workers)
     h = ctypes.c_void_p()
     rc = L.oracle_run(ctypes.byref(inp), ctypes.byref(h))
     if rc != 0:

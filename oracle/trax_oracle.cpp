@@ -113,11 +113,13 @@ struct Ctx {
 };
 
 float min_radius_curvature(float minPt) {
-  // TripletConfiguration.cpp:36-43 with IDEAL_BZ (TripletConfiguration.h:70)
+  // TripletConfiguration.cpp:36-43: the double IDEAL_BZ (TripletConfiguration.h:70)
+  // passes through minRadiusCurvature's float Bz parameter (:56-64)
   const double IDEAL_BZ = 3.8112;
+  const float Bz = (float)IDEAL_BZ;
   const double Q = 1.602177E-19;
   const double GEV_C = 5.344286E-19;
-  return (float)(minPt * GEV_C / (IDEAL_BZ * Q) * 1E2);
+  return (float)(minPt * GEV_C / (Bz * Q) * 1E2);
 }
 
 // ----------------------------------------------------------------- grid

@@ -16,7 +16,9 @@ import pytest
 
 from trax_gb300 import events
 
-REF = "/root/reference"
+from oracle.ref_extract import reference_dir
+
+REF = reference_dir()  # where the reference's sources are read in this container; absent on the GPU machine
 TTBAR = os.path.join(REF, "plotting/data/physics/hits.ttBar.pb")
 GOLDEN_TTBAR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ttbar10_loaded.npz")
 

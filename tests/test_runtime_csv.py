@@ -1,9 +1,10 @@
 """Runtime records in the reference's csv layout."""
 import os
 
+from oracle.ref_extract import reference_dir
 from trax_gb300 import runtime_csv
 
-REF_CSV = "/root/reference/plotting/data/runtime/runtime.bigOne.local.conf.events.100.test.gpu.csv"
+REF_CSV = os.path.join(reference_dir(), "plotting/data/runtime/runtime.bigOne.local.conf.events.100.test.gpu.csv")
 
 
 def _timings(scale=1.0):

@@ -255,11 +255,14 @@ void kmark(trax_ctx* c, int k, bool end) {
 uint32_t* dev_err(trax_ctx* c) { return slot(c, S_ERR); }
 
 float min_radius_curvature(float minPt) {
-  // TripletConfiguration.cpp:36-43 with IDEAL_BZ = 3.8112 (TripletConfiguration.h:70)
+  // TripletConfiguration.cpp:36-43: minRadiusCurvature(minPt, Bz) takes Bz as
+  // a float, so the double IDEAL_BZ = 3.8112 (TripletConfiguration.h:56-70) is
+  // rounded to float before the double arithmetic.
   const double IDEAL_BZ = 3.8112;
+  const float Bz = (float)IDEAL_BZ;
   const double Q = 1.602177E-19;
   const double GEV_C = 5.344286E-19;
-  return (float)(minPt * GEV_C / (IDEAL_BZ * Q) * 1E2);
+  return (float)(minPt * GEV_C / (Bz * Q) * 1E2);
 }
 
 // Device configuration from the host-side settings.  The grid build needs
