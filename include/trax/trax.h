@@ -148,11 +148,37 @@ int trax_set_tracklets(trax_ctx* ctx, const uint32_t* h1, const uint32_t* h2, co
 /* TripletConnectivityTight::run (TripletConnectivityTight.h:42-44, .cpp:5-475). */
 int trax_connectivity(trax_ctx* ctx, float d_eta_cut, uint64_t* n_links);
 
-/* TrackletCircleFitter::run (TrackletCircleFitter.h:25-29, .cpp:3-49). */
+/* TrackletCircleFitter::run (TrackletCircleFitter.h:25-29, .cpp:3-49) on the
+ * connectable list of the last trax_connectivity. */
 int trax_circle_fit(trax_ctx* ctx);
 
-/* CellularAutomaton::run (CellularAutomaton.h:43-49, .cpp:7-465). */
+/* TrackletCircleFitter::run with the caller's validIdx list
+ * (TrackletCircleFitter.h:25-29: `validTrackletsIndices`): the circle radius
+ * of each listed triplet of the context's current triplet set (from the
+ * filter or trax_set_tracklets), 0 for the others; read it with
+ * trax_get_pt.  Indices must be below the number of triplets. */
+int trax_circle_fit_on(trax_ctx* ctx, const uint32_t* valid_idx, uint64_t n_valid);
+/* The pt of the current triplet set (n_triplets floats), after
+ * trax_circle_fit, trax_circle_fit_on or trax_seed_batch with linking. */
+int trax_get_pt(trax_ctx* ctx, float* pt);
+
+/* CellularAutomaton::run (CellularAutomaton.h:43-49, .cpp:7-465) on the
+ * links and pt of the last trax_connectivity / trax_circle_fit. */
 int trax_cellular_automaton(trax_ctx* ctx, uint64_t* n_track_entries);
+
+/* CellularAutomaton::run on the caller's inputs (CellularAutomaton.h:43-49:
+ * tripletsBasis, tripletsFollowers, tripletsPt): n_links links
+ * basis[i] -> follower[i] between triplets 0 .. n_triplets-1 and one pt per
+ * triplet.  Any link set is accepted: the forward phase runs the reference's
+ * iteration (CellularAutomaton.cpp:37-98) until no cell lives, so links need
+ * not go from one layer triplet to the next; a set with a cycle never
+ * settles in the reference and returns TRAX_ERR_ARG here.  Ties of the best
+ * basis go to the lowest basis index.  When the context holds triplets,
+ * n_triplets must equal their number; otherwise the context takes
+ * n_triplets as its triplet count for this run.  Results: trax_get_tracks
+ * (states, the track collection and its per-triplet offsets). */
+int trax_cellular_automaton_on(trax_ctx* ctx, const uint32_t* basis, const uint32_t* follower, uint64_t n_links,
+                               const float* pt, uint64_t n_triplets, uint64_t* n_track_entries);
 
 /* PrefixSum::run (PrefixSum.h:43-44, PrefixSum.cpp:8-36): exclusive uint32
  * scan of `n` elements of the host array `data` in place (round trip through
@@ -173,16 +199,38 @@ int trax_prefix_sum(trax_ctx* ctx, uint32_t* data, uint64_t n);
  *     4096-element tile) is a fixed array inside the library, present on
  *     every GPU that loads it until the process exits; n is therefore limited
  *     to TRAX_NOALLOC_SCAN_MAX elements, larger n returns TRAX_ERR_ARG.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream capture.
+ *   - Every call looks up the array's device address in the current context
+ *     (cudaGetSymbolAddress), so a device reset or another current context
+ *     is picked up.  The first call in a context also loads the library's
+ *     device code there: make that first call before any stream capture.
  *   - All calls share the array and each call clears what it uses; calls
  *     whose work overlaps on the GPU (other streams, other host threads) race.
- *   - The call waits for its stream to finish, so that a timed-out look-back
- *     wait is reported (TRAX_ERR_TIMEOUT).
+ *   - Before returning, the call copies the scan's error word to the host and
+ *     synchronises `stream`, so that a timed-out look-back wait is reported
+ *     (TRAX_ERR_TIMEOUT).
  * A message is written to err_msg (err_len bytes, may be NULL) on failure. */
 #define TRAX_NOALLOC_SCAN_MAX (16ull * 1024ull * 1024ull)
 int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, uint64_t n, void* stream, char* err_msg,
                             size_t err_len);
+
+/* Bounded device waits.  No counterpart in the reference, whose recursive
+ * scan (PrefixSum.cpp:73-140) has no waits between work-groups.  Every
+ * single-pass scan's look-back wait gives up after a number of polls
+ * (default 2^22, each at least 64 ns), records the timeout and finishes; the
+ * call then returns TRAX_ERR_TIMEOUT.
+ * trax_set_wait_limit: polls per wait for the scans this context launches
+ *   afterwards (0 restores the default).  A CUDA graph captured before keeps
+ *   its old limit until trax_seed_batch recaptures, which it does when the
+ *   setting changes.
+ * trax_debug_skip_publish: a host-set fault for testing that path without a
+ *   GPU fault: look-back tile `tile` (4096 elements each) of every later scan
+ *   of this context publishes nothing, so the waits of the tiles after it run
+ *   out and the call returns TRAX_ERR_TIMEOUT.  0xffffffff turns it off.
+ * trax_noalloc_set_wait: the same two settings for trax_prefix_sum_noalloc,
+ *   process-wide (it has no context). */
+int trax_set_wait_limit(trax_ctx* ctx, uint32_t polls);
+int trax_debug_skip_publish(trax_ctx* ctx, uint32_t tile);
+int trax_noalloc_set_wait(uint32_t polls, uint32_t skip_tile);
 
 /* Threads per block of the pair, prediction and filter kernels (multiples of
  * 32 in [32, 256]; defaults 128, 128, 256).  No counterpart in the reference,

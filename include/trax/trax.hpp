@@ -238,6 +238,20 @@ class GeometrySupplement {
   std::vector<float> minR_, maxR_;
 };
 
+// DetectorGeometry (DetectorGeometry.h:17-41) and Dictionary
+// (Dictionary.h:16-38): the detector-id -> radius tables
+// (configs/detectorRadius.dat, radiusDictionary.dat).  The reference passes
+// both to its prediction kernels, which never read them
+// (TripletThetaPhiPredictor.h:44-47, 54-55); they are kept for the call
+// surface.
+struct DetectorGeometry {
+  std::vector<uint32_t> detectorId, detectorLayer;
+  std::vector<uint8_t> radiusDict;  // index into Dictionary::radius
+};
+struct Dictionary {
+  std::vector<float> radius;
+};
+
 // HitCollection (HitCollection.h:23-62): the seven hit columns, sorted by
 // event then layer.  GridBuilder::run reorders it into grid order, like the
 // reference's download of the permuted hits (GridBuilder.cpp:151).
@@ -379,7 +393,9 @@ class TrackletCollection {
   std::vector<uint32_t> trackletOffsets;
   size_t size() const { return hit1.size(); }
   const std::vector<uint32_t>& getTrackletOffsets() const { return trackletOffsets; }
-  uint64_t generation = 0;
+  // chain state of the Context that holds these triplets on the device (a
+  // record of where the collection lives, updated by const run() methods too)
+  mutable uint64_t generation = 0;
 };
 
 // ------------------------------------------------------------ algorithms
@@ -450,13 +466,16 @@ inline void expect_current(const Context& ctx, uint64_t gen, const char* what) {
 }
 }  // namespace detail
 
-// TripletThetaPhiPredictor::run (TripletThetaPhiPredictor.h:44-47, .cpp:10-168).
+// TripletThetaPhiPredictor::run (TripletThetaPhiPredictor.h:44-47, .cpp:10-168),
+// with the reference's parameter list; the geometry tables are unused, as
+// in the reference's kernels.
 class TripletThetaPhiPredictor : public KernelWrapper {
  public:
   using KernelWrapper::KernelWrapper;
-  std::unique_ptr<Pairing> run(HitCollection& /*hits*/, const GeometrySupplement& /*geom*/, int /*nThreads*/,
-                               const TripletConfigurations& layerTriplets, const Grid& /*grid*/, const Pairing& pairs,
-                               bool /*printInfo*/ = false) {
+  std::unique_ptr<Pairing> run(HitCollection& /*hits*/, const DetectorGeometry& /*geom*/,
+                               const GeometrySupplement& /*geomSupplement*/, const Dictionary& /*dict*/,
+                               int /*nThreads*/, const TripletConfigurations& layerTriplets, const Grid& /*grid*/,
+                               const Pairing& pairs, bool /*printInfo*/ = false) {
     detail::expect_current(ctx, pairs.generation, "the pairing");
     uint64_t n = 0;
     ctx.check(trax_triplet_predict(ctx.get(), &n));
@@ -530,49 +549,55 @@ class TripletConnectivityTight : public KernelWrapper {
 };
 
 // TrackletCircleFitter::run (TrackletCircleFitter.h:25-29, .cpp:3-49): the
-// circle radius of every triplet in validIdx (the connectable list of the
-// last connectivity run); other entries are 0.
+// circle radius of every triplet listed in validIdx, 0 for the others.
+// Tracklets this Context did not produce (any TrackletCollection over `hits`
+// in input order) are uploaded first; validIdx may be any list of their
+// indices.
 class TrackletCircleFitter : public KernelWrapper {
  public:
   using KernelWrapper::KernelWrapper;
   std::unique_ptr<std::vector<float>> run(const HitCollection& /*hits*/, const TrackletCollection& tracklets,
                                           const std::vector<uint32_t>& validIdx, uint32_t /*nThreads*/,
                                           bool /*printInfo*/ = false) {
-    detail::expect_current(ctx, tracklets.generation, "the tracklet collection");
-    trax_batch_stats s;
-    ctx.check(trax_get_stats(ctx.get(), &s));
-    if (validIdx.size() != s.n_connectable)
-      throw Error(TRAX_ERR_STATE, "validIdx is not the connectable list of the last connectivity run");
-    ctx.check(trax_circle_fit(ctx.get()));
-    ctx.bump();
-    std::vector<float> eta(tracklets.size());
+    if (tracklets.generation != ctx.generation()) {
+      ctx.check(trax_set_tracklets(ctx.get(), tracklets.hit1.data(), tracklets.hit2.data(), tracklets.hit3.data(),
+                                   tracklets.size()));
+      tracklets.generation = ctx.bump();
+    }
+    ctx.check(trax_circle_fit_on(ctx.get(), validIdx.data(), validIdx.size()));
     std::unique_ptr<std::vector<float>> pt(new std::vector<float>(tracklets.size()));
-    ctx.check(trax_get_triplet_eta_pt(ctx.get(), eta.data(), pt->data()));
+    ctx.check(trax_get_pt(ctx.get(), pt->data()));
     return pt;
   }
 };
 
-// CellularAutomaton::run (CellularAutomaton.h:43-49, .cpp:7-465): the track
-// collection and its per-triplet offsets.
+// CellularAutomaton::run (CellularAutomaton.h:43-49, .cpp:7-465) on the
+// caller's links basis[i] -> followers[i] and one pt per triplet: the track
+// collection and its per-triplet offsets.  Any acyclic link set is accepted.
+// The connectable list is taken for the call surface; the reference's CA
+// reads it only for its debug printout.  The CA's states are kept for
+// states().
 class CellularAutomaton : public KernelWrapper {
  public:
   using KernelWrapper::KernelWrapper;
   std::tuple<std::unique_ptr<std::vector<uint32_t>>, std::unique_ptr<std::vector<uint32_t>>> run(
-      const std::vector<uint32_t>& basis, const std::vector<uint32_t>& /*followers*/,
-      const std::vector<float>& pt, const std::vector<uint32_t>& /*connectable*/, uint32_t /*nThreads*/,
-      bool /*printInfo*/ = false) {
-    trax_batch_stats s;
-    ctx.check(trax_get_stats(ctx.get(), &s));
-    if (basis.size() != s.n_links) throw Error(TRAX_ERR_STATE, "basis is not the link list of the last run");
+      const std::vector<uint32_t>& basis, const std::vector<uint32_t>& followers, const std::vector<float>& pt,
+      const std::vector<uint32_t>& /*connectable*/, uint32_t /*nThreads*/, bool /*printInfo*/ = false) {
+    if (basis.size() != followers.size()) throw Error(TRAX_ERR_ARG, "basis and followers differ in length");
     uint64_t n = 0;
-    ctx.check(trax_cellular_automaton(ctx.get(), &n));
+    ctx.check(trax_cellular_automaton_on(ctx.get(), basis.data(), followers.data(), basis.size(), pt.data(),
+                                         pt.size(), &n));
     ctx.bump();
     std::unique_ptr<std::vector<uint32_t>> tracks(new std::vector<uint32_t>(n));
     std::unique_ptr<std::vector<uint32_t>> offsets(new std::vector<uint32_t>(pt.size() + 1));
-    std::vector<uint32_t> states(pt.size());
-    ctx.check(trax_get_tracks(ctx.get(), states.data(), tracks->data(), offsets->data()));
+    states_.assign(pt.size(), 0);
+    ctx.check(trax_get_tracks(ctx.get(), states_.data(), tracks->data(), offsets->data()));
     return std::make_tuple(std::move(tracks), std::move(offsets));
   }
+  const std::vector<uint32_t>& states() const { return states_; }
+
+ private:
+  std::vector<uint32_t> states_;
 };
 
 // PrefixSum::run (PrefixSum.h:43-44): exclusive uint32 scan in place, the

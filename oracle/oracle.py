@@ -227,6 +227,33 @@ def link(x, y, z, layer, event, h1, h2, h3, n_events: int, n_lt: int, d_eta_cut:
         L.oracle_free(h)
 
 
+def ca(n_triplets: int, basis, follower, pt) -> Dict[str, np.ndarray]:
+    """CellularAutomaton::run alone on given links and pt."""
+    L = lib()
+    if not hasattr(L, "_ca_ready"):
+        L.oracle_ca.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                ctypes.POINTER(ctypes.c_void_p)]
+        L.oracle_ca.restype = ctypes.c_int
+        L._ca_ready = True
+    b = np.ascontiguousarray(basis, dtype=np.uint32)
+    f = np.ascontiguousarray(follower, dtype=np.uint32)
+    p = np.ascontiguousarray(pt, dtype=np.float32)
+    h = ctypes.c_void_p()
+    if L.oracle_ca(n_triplets, _ptr(b), _ptr(f), b.size, _ptr(p), ctypes.byref(h)) != 0:
+        raise OracleError(L.oracle_last_error().decode())
+    try:
+        d = {}
+        for name in ("ca_states", "ca_best", "tracks", "track_offsets", "stats"):
+            n = L.oracle_size(h, 0, name.encode())
+            a = np.zeros(max(n, 1), dtype=np.uint32)
+            L.oracle_copy(h, 0, name.encode(), _ptr(a))
+            d[name] = a[:n]
+        d["stats_dict"] = {k: int(v) for k, v in zip(STATS, d["stats"])}
+        return d
+    finally:
+        L.oracle_free(h)
+
+
 def prefix_sum_blelloch(data: np.ndarray, wg: int) -> np.ndarray:
     a = np.ascontiguousarray(data, dtype=np.uint32).copy()
     lib().oracle_prefix_sum_blelloch(_ptr(a), a.size, wg)

@@ -63,6 +63,9 @@ def lib():
             L.ref_copy.restype = ctypes.c_int
             L.ref_free.argtypes = [ctypes.c_void_p]
             L.ref_prefix_sum.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]
+            L.ref_ca.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                 ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
+            L.ref_ca.restype = ctypes.c_int
             _lib = L
         return _lib
 
@@ -87,6 +90,30 @@ def run(batch, n_threads: int = 1, local_mem: int = GTX660_LOCAL_MEM, max_ca_ite
                 continue
             dt = np.float32 if name in FLOAT_ARRAYS else np.uint32
             a = np.zeros(max(n, 1), dtype=dt)
+            L.ref_copy(h, name.encode(), a.ctypes.data)
+            out[name] = a[:n]
+        out["stats_dict"] = {k: int(v) for k, v in zip(STATS, out["stats"])}
+        return out
+    finally:
+        L.ref_free(h)
+
+
+def ca(n_triplets: int, basis, follower, pt, n_threads: int = 1, max_ca_iterations: int = 100000
+       ) -> Dict[str, np.ndarray]:
+    """The reference's CA kernels alone on given links and pt."""
+    L = lib()
+    b = np.ascontiguousarray(basis, dtype=np.uint32)
+    f = np.ascontiguousarray(follower, dtype=np.uint32)
+    p = np.ascontiguousarray(pt, dtype=np.float32)
+    h = ctypes.c_void_p()
+    if L.ref_ca(n_triplets, b.ctypes.data, f.ctypes.data, b.size, p.ctypes.data, n_threads, max_ca_iterations,
+                ctypes.byref(h)) != 0:
+        raise RuntimeError(L.ref_last_error().decode())
+    try:
+        out: Dict[str, np.ndarray] = {}
+        for name in ("ca_states", "ca_best", "tracks", "track_offsets", "stats"):
+            n = L.ref_size(h, name.encode())
+            a = np.zeros(max(n, 1), dtype=np.uint32)
             L.ref_copy(h, name.encode(), a.ctypes.data)
             out[name] = a[:n]
         out["stats_dict"] = {k: int(v) for k, v in zip(STATS, out["stats"])}

@@ -792,6 +792,33 @@ int ref_run(const oracle_input* in, uint32_t n_threads, uint32_t local_mem_bytes
   return 0;
 }
 
+// CellularAutomaton::run alone (CellularAutomaton.h:43-49, .cpp:7-465) on
+// given links and pt, with exec.threads = n_threads.
+int ref_ca(uint32_t n_triplets, const uint32_t* basis, const uint32_t* follower, uint32_t n_links, const float* pt,
+           uint32_t n_threads, uint32_t max_ca_iterations, ref_result** out) {
+  *out = nullptr;
+  if (n_threads == 0 || n_triplets == 0 || n_links == 0) {
+    g_error = "the CA needs triplets, links and work-items";
+    return -1;
+  }
+  Run R;
+  R.T = n_threads;
+  R.basis = upload(basis, n_links, kUninit);
+  R.follower = upload(follower, n_links, kUninit);
+  R.pt = upload(pt, n_triplets, uninit_f());
+  cellular_automaton(R, max_ca_iterations);
+  auto* res = new ref_result;
+  auto& A = res->arrays;
+  A["ca_states"] = words(R.states);
+  A["ca_best"] = words(R.best);
+  A["tracks"] = words(R.tracks);
+  A["track_offsets"] = words(R.trackOffsets);
+  A["stats"] = {R.st.pair_sentinels, R.st.cand_sentinels, R.st.ca_iterations,     R.st.no_links,
+                R.st.ca_chain_broken, R.st.grid_count_local, R.st.grid_store_variant, R.st.pair_count_local};
+  *out = res;
+  return 0;
+}
+
 const char* ref_last_error(void) { return g_error.c_str(); }
 
 int64_t ref_size(const ref_result* r, const char* name) {

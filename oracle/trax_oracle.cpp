@@ -1047,6 +1047,43 @@ int oracle_link(const oracle_link_input* in, oracle_result** out) {
   return 0;
 }
 
+// CellularAutomaton::run (CellularAutomaton.h:43-49, .cpp:7-465) alone, on
+// given links basis[i] -> follower[i] over n_triplets triplets and one pt per
+// triplet (the caller-input form of the CA).
+int oracle_ca(uint32_t n_triplets, const uint32_t* basis, const uint32_t* follower, uint32_t n_links,
+              const float* pt, oracle_result** out) {
+  *out = nullptr;
+  for (uint32_t p = 0; p < n_links; ++p) {
+    if (basis[p] >= n_triplets || follower[p] >= n_triplets) {
+      set_error("link triplet index out of range");
+      return -1;
+    }
+  }
+  ConnOut co;
+  co.basis.assign(basis, basis + n_links);
+  co.follower.assign(follower, follower + n_links);
+  co.noLinks = n_links == 0;
+  std::vector<float> p(pt, pt + n_triplets);
+  CAOut ca;
+  cellular_automaton(n_triplets, co, p, ca);
+  oracle_result* r = new oracle_result();
+  r->groups.resize(1);
+  Group& G = r->groups[0];
+  G.u("ca_states") = ca.states;
+  G.u("ca_best") = ca.best;
+  G.u("tracks") = ca.tracks;
+  G.u("track_offsets") = ca.trackOffsets;
+  std::vector<uint>& st = G.u("stats");
+  st.assign(ST_N, 0u);
+  st[ST_TRIPLETS] = n_triplets;
+  st[ST_LINKS] = n_links;
+  st[ST_CA_ITER] = ca.iterations;
+  st[ST_CA_CAPPED] = ca.capped ? 1u : 0u;
+  st[ST_TRACK_ENTRIES] = (uint)ca.tracks.size();
+  *out = r;
+  return 0;
+}
+
 void oracle_free(oracle_result* r) { delete r; }
 
 uint32_t oracle_n_groups(const oracle_result* r) { return (uint32_t)r->groups.size(); }

@@ -78,6 +78,9 @@ typedef struct oracle_link_input {
   float d_eta_cut;
 } oracle_link_input;
 int oracle_link(const oracle_link_input* in, oracle_result** out);
+// CellularAutomaton::run alone on given links and pt (n_triplets values).
+int oracle_ca(uint32_t n_triplets, const uint32_t* basis, const uint32_t* follower, uint32_t n_links,
+              const float* pt, oracle_result** out);
 void oracle_free(oracle_result* r);
 const char* oracle_last_error(void);
 

@@ -100,7 +100,9 @@ int main(int argc, char** argv) {
   trax::CellularAutomaton ca(ctx);
   gridBuilder.run(hits, 256, es, ls, grid);
   auto pairs = pairGen.run(hits, geom, 256, lts, grid);
-  auto cands = predictor.run(hits, geom, 256, lts, grid, *pairs);
+  trax::DetectorGeometry detGeom;
+  trax::Dictionary dict;
+  auto cands = predictor.run(hits, detGeom, geom, dict, 256, lts, grid, *pairs);
   auto tracklets = filter.run(hits, grid, *pairs, *cands, 256, lts);
   auto links = connectivity.run(hits, *tracklets, lts, 0.0256f, 256);
   std::unique_ptr<std::vector<float>> pt;

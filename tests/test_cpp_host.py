@@ -41,6 +41,25 @@ def test_host_class_chain_equals_batched_call(tmp_path):
     assert r.stdout.startswith("OK host classes")
 
 
+@pytest.mark.gpu
+def test_ca_class_on_caller_links_and_pt(tmp_path):
+    """CellularAutomaton::run computes on the links and pt it is given (the
+    reference's connectivity fixture plus hand-made pt), on a Context without
+    triplets of its own."""
+    from trax_gb300 import build
+    build.build()
+    exe = _compile(tmp_path, os.path.dirname(build.LIB_PATH), os.path.join(REPO, "tests", "cpp", "ca_inputs_test.cpp"))
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("OK ca inputs")
+
+
+def test_ca_inputs_program_compiles(tmp_path):
+    from trax_gb300 import build
+    build.build()
+    _compile(tmp_path, os.path.dirname(build.LIB_PATH), os.path.join(REPO, "tests", "cpp", "ca_inputs_test.cpp"))
+
+
 def test_loader_classes_equal_the_c_loader(tmp_path):
     """trax::EventFile + trax::addEvents (the reference's HitCollection::addEvent
     per event of a PEventContainer) give the columns, supplements and findable

@@ -191,3 +191,20 @@ def test_work_group_sizes_give_the_same_sets(n_threads):
         assert cr[k] == co[k], k
     assert np.array_equal(r["pair_offsets"], o["pair_offsets"])
     assert np.array_equal(r["trip_offsets"], o["trip_offsets"])
+
+
+# ------------------------------------------------- the CA alone, any link set
+@pytest.mark.parametrize("seed,sort_by_basis,n_threads", [(1, True, 1), (2, False, 1), (3, True, 64),
+                                                          (4, False, 256)])
+def test_ca_on_random_link_sets_identical(seed, sort_by_basis, n_threads):
+    """CellularAutomaton::run on links that skip levels, with many bases per follower,
+    repeated links and ties of |dpt|: the reference's kernels and the oracle agree."""
+    from tests.ca_cases import random_links
+    b, f, pt = random_links(seed, sort_by_basis=sort_by_basis)
+    n = pt.size
+    r = ref.ca(n, b, f, pt, n_threads=n_threads)
+    o = oracle.ca(n, b, f, pt)
+    assert r["stats_dict"]["ca_chain_broken"] == 0 and o["stats_dict"]["ca_capped"] == 0
+    assert r["stats_dict"]["ca_iterations"] == o["stats_dict"]["ca_iterations"] > 3
+    for name in ("ca_states", "ca_best", "tracks", "track_offsets"):
+        assert np.array_equal(r[name], o[name]), name

@@ -34,7 +34,8 @@ EXPORTED = [
     "trax_apply_alignment", "trax_events_read", "trax_events_free", "trax_events_raw", "trax_events_load",
     "trax_events_upload", "trax_physics_triplets_device", "trax_physics_tracks_device",
     "trax_physics_triplets", "trax_physics_tracks", "trax_geometry_from_files", "trax_host_alloc",
-    "trax_host_free",
+    "trax_host_free", "trax_set_wait_limit", "trax_debug_skip_publish", "trax_noalloc_set_wait",
+    "trax_circle_fit_on", "trax_get_pt", "trax_cellular_automaton_on",
 ]
 
 
@@ -121,6 +122,12 @@ def load() -> ctypes.CDLL:
             "trax_circle_fit": ([vp], i32),
             "trax_cellular_automaton": ([vp, pu64], i32),
             "trax_prefix_sum": ([vp, vp, u64], i32),
+            "trax_set_wait_limit": ([vp, u32], i32),
+            "trax_circle_fit_on": ([vp, vp, u64], i32),
+            "trax_get_pt": ([vp, vp], i32),
+            "trax_cellular_automaton_on": ([vp, vp, vp, u64, vp, u64, pu64], i32),
+            "trax_debug_skip_publish": ([vp, u32], i32),
+            "trax_noalloc_set_wait": ([u32, u32], i32),
             "trax_seed_batch": ([vp, vp, vp], i32),
             "trax_get_stats": ([vp, vp], i32),
             "trax_get_timings": ([vp, vp, vp], i32),
@@ -305,6 +312,25 @@ class Context:
     def cellular_automaton(self) -> int:
         return self._count(self._L.trax_cellular_automaton)
 
+    def circle_fit_on(self, valid_idx) -> np.ndarray:
+        """TrackletCircleFitter::run on the caller's index list; returns pt of every triplet."""
+        idx = np.ascontiguousarray(valid_idx, dtype=np.uint32)
+        self._check(self._L.trax_circle_fit_on(self._h, _p(idx) if idx.size else None, idx.size))
+        n = self.stats().n_triplets
+        pt = np.zeros(max(n, 1), dtype=np.float32)
+        self._check(self._L.trax_get_pt(self._h, _p(pt)))
+        return pt[:n]
+
+    def cellular_automaton_on(self, basis, follower, pt):
+        """CellularAutomaton::run on the caller's links and pt; returns (states, tracks, track offsets)."""
+        b = np.ascontiguousarray(basis, dtype=np.uint32)
+        f = np.ascontiguousarray(follower, dtype=np.uint32)
+        p = np.ascontiguousarray(pt, dtype=np.float32)
+        n = ctypes.c_uint64()
+        self._check(self._L.trax_cellular_automaton_on(self._h, _p(b), _p(f), b.size, _p(p), p.size,
+                                                        ctypes.byref(n)))
+        return self.tracks()
+
     def seed_batch(self, use_graph: bool = True, run_linking: bool = True, d_eta_cut: float = 0.0256) -> BatchStats:
         opts = BatchOptsC(int(use_graph), int(run_linking), d_eta_cut)
         st = BatchStatsC()
@@ -391,6 +417,12 @@ class Context:
         k = np.zeros(len(self.KERNELS), dtype=np.float32)
         self._check(self._L.trax_get_timings(self._h, _p(s), _p(k)))
         return dict(zip(self.STAGES, s.tolist())), dict(zip(self.KERNELS, k.tolist()))
+
+    def set_wait_limit(self, polls: int = 0, skip_publish_tile: int = 0xFFFFFFFF):
+        """Bounded-wait settings of this context's scans: polls per look-back wait
+        (0: the default) and a tile that publishes nothing (a test fault; 0xffffffff: none)."""
+        self._check(self._L.trax_set_wait_limit(self._h, polls))
+        self._check(self._L.trax_debug_skip_publish(self._h, skip_publish_tile))
 
     def prefix_sum(self, data: np.ndarray) -> np.ndarray:
         a = np.ascontiguousarray(data, dtype=np.uint32).copy()

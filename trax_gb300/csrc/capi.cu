@@ -70,8 +70,11 @@ enum Slot {
   S_PRED_WARPS,
   S_FLAG_WORDS,
   S_CONN_WORDS,
+  S_USER,    // length of a caller-provided list (trax_circle_fit_on)
+  S_LIVING,  // living flag of the caller-link CA iteration
   S_N
 };
+static_assert(S_N <= 64, "the slot buffers hold 64 words");
 
 enum Mode { SYNCED, DEVICE };
 
@@ -129,6 +132,7 @@ struct trax_ctx {
   // connectivity / fit / CA
   DevBuf eta, segOf, segStart, linkCount, linkRun, cflags, basis, follower, connS, nonConnS, connW, nonConnW, connIdx, nonConnIdx, pt;
   DevBuf states, inStart, inCursor, inList, best, isBest, handlers, tracks;
+  DevBuf userIdx, caNext;  // caller-provided fit list; second state buffer of the caller-link CA
   // bookkeeping
   DevBuf scanScratch, slots;
   uint32_t* hSlots = nullptr;  // pinned copy of the slots
@@ -149,6 +153,7 @@ struct trax_ctx {
   cudaGraphExec_t graphExec = nullptr;
   uint64_t graphKey = 0;
   uint64_t bufGeneration = 0;
+  trax::WaitCtl wait;  // bounded-wait settings of every scan (trax_set_wait_limit, trax_debug_skip_publish)
   uint32_t graphLaunches = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double lastMs = 0.0;
@@ -159,6 +164,10 @@ struct trax_ctx {
   uint64_t nFit = 0;
   bool fitReady = false;
   uint64_t tripGen = 1, fitTripGen = 0;  // generation of the triplet set
+  // pt and CA results valid for triplet set ptGen / caGen (set by the stages
+  // and by the caller-input entry points)
+  uint64_t ptGen = 0, caGen = 0;
+  bool caOnly = false;  // triplet count taken from the CA's caller input, no triplet arrays
   float fitSigmaTip[TRAX_MAX_LT] = {};
   cudaEvent_t stageEv[N_STAGES + 1] = {};
 
@@ -375,7 +384,7 @@ int scan_publish(trax_ctx* c, Mode mode, uint32_t* data, uint64_t nHost, const u
   else if (scan_scratch_bytes(maxN) > c->scanScratch.cap)
     return fail(c, TRAX_ERR_STATE, "device-mode scan scratch too small");
   CK(scan_exclusive(data, data, nHost + 1, nDev, 1, maxN, c->scanScratch.p, dev_err(c), c->st, &c->launches,
-                    true));
+                    true, c->wait));
   CK(publish_total(data, nDev, nHost, cap, slot(c, dst), dev_err(c), c->st, &c->launches));
   return TRAX_OK;
 }
@@ -646,7 +655,7 @@ int stage_ca(trax_ctx* c, Mode mode) {
   // in-degree prefix (its total is the number of links; not published)
   if (mode == SYNCED) CK(ensure(c, c->scanScratch, scan_scratch_bytes(maxT + 1)));
   CK(scan_exclusive(b.inStart, b.inStart, c->nT + 1, mode == DEVICE ? nTDev : nullptr, 1, maxT + 1,
-                    c->scanScratch.p, dev_err(c), c->st, &c->launches, true));
+                    c->scanScratch.p, dev_err(c), c->st, &c->launches, true, c->wait));
   CK(ca_fill(ptr<uint32_t>(c->basis), ptr<uint32_t>(c->follower), nLinksDev, maxLinks, b, nTDev, maxT, c->st,
              &c->launches));
   CK(ca_forward(c->cfg, b, nTDev, maxT, c->st, &c->launches));
@@ -697,6 +706,9 @@ int run_stage(trax_ctx* c, int stage) {
   RC(check_device_error(c));
   c->stage = stage;
   if (stage == 4) ++c->tripGen;
+  if (stage == 6) c->ptGen = c->tripGen;
+  if (stage == 7) c->caGen = c->tripGen;
+  c->caOnly = false;
   return TRAX_OK;
 }
 
@@ -769,6 +781,7 @@ uint64_t shape_key(trax_ctx* c, bool linking) {
   mix(c->maxLayerHits > 0xffffu ? 1 : 0);  // the grid build's 16-bit counters hold layers below 65 536 hits
   mix(c->bufGeneration); mix(c->capTasks); mix(c->capPairs); mix(c->capCands); mix(c->capT); mix(c->capLinks);
   mix(c->capTracks);
+  mix(c->wait.spinLimit); mix(c->wait.skipTile);  // captured into the scans' launch arguments
   const unsigned char* b = reinterpret_cast<const unsigned char*>(&c->cfg);
   for (size_t i = 0; i < sizeof(DevConfig); ++i) mix(b[i]);
   return k;
@@ -1196,6 +1209,7 @@ int trax_set_tracklets(trax_ctx* c, const uint32_t* h1, const uint32_t* h2, cons
   RC(check_device_error(c));
   c->stage = 4;
   ++c->tripGen;
+  c->caOnly = false;
   return TRAX_OK;
 }
 
@@ -1238,6 +1252,120 @@ int trax_cellular_automaton(trax_ctx* c, uint64_t* n_track_entries) {
   return TRAX_OK;
 }
 
+int trax_circle_fit_on(trax_ctx* c, const uint32_t* valid_idx, uint64_t n_valid) {
+  if (!c || (n_valid && !valid_idx)) return fail(c, TRAX_ERR_ARG, "null index list");
+  if (c->stage < 4 || c->caOnly) return fail(c, TRAX_ERR_STATE, "no triplets: run the filter or trax_set_tracklets");
+  const uint64_t nT = c->nT;
+  for (uint64_t i = 0; i < n_valid; ++i)
+    if (valid_idx[i] >= nT) return fail(c, TRAX_ERR_ARG, "triplet index out of range");
+  CK(cudaSetDevice(c->device));
+  const Mode mode = SYNCED;
+  ENSURE(userIdx, n_valid, 4);
+  ENSURE(pt, nT, 4);
+  if (n_valid) CK(cudaMemcpyAsync(c->userIdx.p, valid_idx, n_valid * 4, cudaMemcpyHostToDevice, c->st));
+  c->hSlots[S_USER] = (uint32_t)n_valid;
+  CK(cudaMemcpyAsync(slot(c, S_USER), c->hSlots + S_USER, 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->pt.p, 0, (size_t)std::max<uint64_t>(nT, 1) * 4, c->st));
+  CK(circle_fit(dev_hits(c), triplets(c, nT), ptr<uint32_t>(c->userIdx), slot(c, S_USER), n_valid,
+                ptr<float>(c->pt), c->st, &c->launches));
+  CK(cudaStreamSynchronize(c->st));
+  RC(check_device_error(c));
+  c->ptGen = c->tripGen;
+  return TRAX_OK;
+}
+
+int trax_get_pt(trax_ctx* c, float* pt) {
+  if (!c || (!pt && c->nT)) return TRAX_ERR_ARG;
+  if (c->ptGen != c->tripGen) return fail(c, TRAX_ERR_STATE, "no circle fit of the current triplets");
+  RC(copy_out(c, pt, c->pt, c->nT * 4));
+  CK(cudaStreamSynchronize(c->st));
+  return TRAX_OK;
+}
+
+int trax_cellular_automaton_on(trax_ctx* c, const uint32_t* basis, const uint32_t* follower, uint64_t n_links,
+                               const float* pt, uint64_t n_triplets, uint64_t* n_track_entries) {
+  if (!c || !basis || !follower || !pt) return fail(c, TRAX_ERR_ARG, "null input");
+  if (n_links == 0 || n_triplets == 0) return fail(c, TRAX_ERR_ARG, "the CA needs links and triplets");
+  if (n_links > 0xfffffff0ull || n_triplets > 0xfffffff0ull) return fail(c, TRAX_ERR_ARG, "input too large");
+  const bool haveTriplets = c->stage >= 4 && !c->caOnly;
+  if (haveTriplets && n_triplets != c->nT)
+    return fail(c, TRAX_ERR_ARG, "pt must hold one value per triplet of the context's triplet set");
+  for (uint64_t p = 0; p < n_links; ++p)
+    if (basis[p] >= n_triplets || follower[p] >= n_triplets)
+      return fail(c, TRAX_ERR_ARG, "link triplet index out of range");
+  CK(cudaSetDevice(c->device));
+  const Mode mode = SYNCED;
+  const uint64_t nT = n_triplets, nL = n_links;
+  if (!haveTriplets) {
+    c->nT = nT;
+    c->caOnly = true;
+    ++c->tripGen;  // a triplet set of its own, without hits
+  }
+  ENSURE(basis, nL, 4);
+  ENSURE(follower, nL, 4);
+  ENSURE(pt, nT, 4);
+  ENSURE(states, nT, 4);
+  ENSURE(caNext, nT, 4);
+  ENSURE(inStart, nT + 1, 4);
+  ENSURE(inCursor, nT, 4);
+  ENSURE(inList, nL, 4);
+  ENSURE(best, nT, 4);
+  ENSURE(isBest, nT, 4);
+  ENSURE(handlers, nT + 1, 4);
+  CK(ensure(c, c->scanScratch, scan_scratch_bytes(nT + 1)));
+  CK(cudaMemcpyAsync(c->basis.p, basis, nL * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->follower.p, follower, nL * 4, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->pt.p, pt, nT * 4, cudaMemcpyHostToDevice, c->st));
+  memset(c->hSlots, 0, sizeof(uint32_t) * S_N);
+  c->hSlots[S_TRIPLETS] = (uint32_t)nT;
+  c->hSlots[S_LINKS] = (uint32_t)nL;
+  CK(cudaMemcpyAsync(c->slots.p, c->hSlots, sizeof(uint32_t) * S_N, cudaMemcpyHostToDevice, c->st));
+  const uint32_t* nTDev = slot(c, S_TRIPLETS);
+  const uint32_t* nLinksDev = slot(c, S_LINKS);
+  CABuffers b = ca_buffers(c);
+  // states 1, in-degrees, the incoming bases of every follower (ascending)
+  CK(ca_in_degree(ptr<uint32_t>(c->follower), nLinksDev, nL, b, nTDev, nT, c->st, &c->launches));
+  CK(scan_exclusive(b.inStart, b.inStart, nT + 1, nullptr, 0, nT + 1, c->scanScratch.p, dev_err(c), c->st,
+                    &c->launches, true, c->wait));
+  CK(ca_fill(ptr<uint32_t>(c->basis), ptr<uint32_t>(c->follower), nLinksDev, nL, b, nTDev, nT, c->st,
+             &c->launches));
+  // forward phase: the reference's iteration (CellularAutomaton.cpp:37-98),
+  // both state buffers starting at 1, swapped without copying; a link set
+  // with a cycle never settles and is rejected after nT + 2 iterations
+  CK(fill_u32(ptr<uint32_t>(c->caNext), 1u, (uint32_t)nT, c->st, &c->launches));
+  uint32_t* cur = ptr<uint32_t>(c->states);
+  uint32_t* next = ptr<uint32_t>(c->caNext);
+  uint32_t* living = slot(c, S_LIVING);
+  uint64_t iterations = 0;
+  uint32_t alive = 0;
+  do {
+    ++iterations;
+    CK(cudaMemsetAsync(living, 0, 4, c->st));
+    CK(ca_iteration(ptr<uint32_t>(c->basis), ptr<uint32_t>(c->follower), (uint32_t)nL, cur, next, living, c->st,
+                    &c->launches));
+    CK(cudaMemcpyAsync(&alive, living, 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    std::swap(cur, next);
+  } while (alive && iterations <= nT + 2);
+  if (alive) return fail(c, TRAX_ERR_ARG, "the links form a cycle: the CA's states never settle");
+  if (cur != ptr<uint32_t>(c->states))
+    CK(cudaMemcpyAsync(c->states.p, cur, nT * 4, cudaMemcpyDeviceToDevice, c->st));
+  // backward phase, handlers and tracks as in the chain
+  CK(ca_backward(ptr<float>(c->pt), b, nTDev, nT, nLinksDev, c->st, &c->launches));
+  RC(scan_publish(c, SYNCED, b.handlers, nT, nullptr, nT, S_TRACKS, NO_CAP));
+  RC(read_slot(c, S_TRACKS, &c->nTracks));
+  ENSURE(tracks, c->nTracks, 4);
+  CK(ca_tracks(b, nTDev, nT, ptr<uint32_t>(c->tracks), c->nTracks, dev_err(c), c->st, &c->launches));
+  CK(cudaStreamSynchronize(c->st));
+  RC(check_device_error(c));
+  c->nLinks = nL;
+  c->noLinks = false;
+  c->nConn = c->nNonConn = 0;
+  c->caGen = c->tripGen;
+  if (n_track_entries) *n_track_entries = c->nTracks;
+  return TRAX_OK;
+}
+
 int trax_prefix_sum(trax_ctx* c, uint32_t* data, uint64_t n) {
   if (!c || (!data && n)) return fail(c, TRAX_ERR_ARG, "null data");
   if (n == 0) return TRAX_OK;
@@ -1250,13 +1378,25 @@ int trax_prefix_sum(trax_ctx* c, uint32_t* data, uint64_t n) {
   if (e == cudaSuccess) e = cudaMemsetAsync(c->slots.p, 0, 4, c->st);
   if (e == cudaSuccess)
     e = scan_exclusive(ptr<uint32_t>(tmp), ptr<uint32_t>(tmp), n, nullptr, 0, n, c->scanScratch.p, dev_err(c), c->st,
-                       &c->launches, false);  // wraps like PrefixSum's uint arithmetic
+                       &c->launches, false, c->wait);  // wraps like PrefixSum's uint arithmetic
   if (e == cudaSuccess) e = cudaMemcpyAsync(data, tmp.p, n * 4, cudaMemcpyDeviceToHost, c->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) rc = cuda_fail(c, e, "trax_prefix_sum");
   release(tmp);
   if (rc == TRAX_OK) rc = check_device_error(c);
   return rc;
+}
+
+int trax_set_wait_limit(trax_ctx* c, uint32_t polls) {
+  if (!c) return TRAX_ERR_ARG;
+  c->wait.spinLimit = polls;
+  return TRAX_OK;
+}
+
+int trax_debug_skip_publish(trax_ctx* c, uint32_t tile) {
+  if (!c) return TRAX_ERR_ARG;
+  c->wait.skipTile = tile;
+  return TRAX_OK;
 }
 
 int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* stats) {
@@ -1331,6 +1471,8 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
     RC(error_from_bits(c, bits));
     c->stage = linking ? 7 : 4;
     ++c->tripGen;
+    if (linking) c->ptGen = c->caGen = c->tripGen;
+    c->caOnly = false;
     fill_stats(c, stats);
     return TRAX_OK;
   }
@@ -1450,9 +1592,9 @@ int trax_physics_tracks_device(trax_ctx* c, uint64_t total_tracks, trax_track_me
   const uint32_t* off = ptr<uint32_t>(c->handlers);
   CK(track_sizes(off, nT, isTrack, hitsOf, c->st));
   CK(scan_exclusive(isTrack, isTrack, (uint64_t)nT + 1, nullptr, 0, (uint64_t)nT + 1, c->scanScratch.p, dev_err(c),
-                    c->st, nullptr, true));
+                    c->st, nullptr, true, c->wait));
   CK(scan_exclusive(hitsOf, hitsOf, (uint64_t)nT + 1, nullptr, 0, (uint64_t)nT + 1, c->scanScratch.p, dev_err(c),
-                    c->st, nullptr, true));
+                    c->st, nullptr, true, c->wait));
   uint32_t totals[2];
   CK(cudaMemcpyAsync(&totals[0], isTrack + nT, 4, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(&totals[1], hitsOf + nT, 4, cudaMemcpyDeviceToHost, c->st));
@@ -1495,7 +1637,7 @@ int trax_physics_tracks_device(trax_ctx* c, uint64_t total_tracks, trax_track_me
   if (!stable) return fail(c, TRAX_ERR_TIMEOUT, "track components did not settle in 64 rounds");
   CK(track_members(t, nTracks, false, c->st));
   CK(scan_exclusive(t.compSize, t.compStart, (uint64_t)nTracks + 1, nullptr, 0, (uint64_t)nTracks + 1,
-                    c->scanScratch.p, dev_err(c), c->st, nullptr, true));
+                    c->scanScratch.p, dev_err(c), c->st, nullptr, true, c->wait));
   CK(track_members(t, nTracks, true, c->st));
   unsigned long long* counts = ptr<unsigned long long>(c->trk_counts);
   CK(track_greedy(t, nTracks, ptr<unsigned long long>(c->trk_table), tableSize - 1, counts, c->st));
@@ -1538,8 +1680,9 @@ int trax_get_links(trax_ctx* c, uint32_t* basis, uint32_t* follower, uint32_t* c
 
 int trax_get_tracks(trax_ctx* c, uint32_t* states, uint32_t* tracks, uint32_t* track_offsets) {
   if (!c) return TRAX_ERR_ARG;
-  if (c->stage >= 5 && c->noLinks) return TRAX_OK;  // no links: the reference runs no CA
-  if (c->stage < 7) return fail(c, TRAX_ERR_STATE, "cellular automaton not run");
+  const bool caOn = c->caGen == c->tripGen;  // also set by trax_cellular_automaton_on
+  if (!caOn && c->stage >= 5 && c->noLinks) return TRAX_OK;  // no links: the reference runs no CA
+  if (!caOn && c->stage < 7) return fail(c, TRAX_ERR_STATE, "cellular automaton not run");
   RC(copy_out(c, states, c->states, c->nT * 4));
   RC(copy_out(c, tracks, c->tracks, c->nTracks * 4));
   RC(copy_out(c, track_offsets, c->handlers, (c->nT + 1) * 4));
@@ -1596,7 +1739,8 @@ int trax_fit_prepare(trax_ctx* c, const trax_fit_opts* opts, uint64_t* n_fit) {
   CK(fit_select(f, c->cfg, dev_hits(c), fit_triplets(c), nT, truthOnly, ok, ptr<uint32_t>(c->fitSegCnt), c->st,
                 &c->launches));
   CK(ensure(c, c->scanScratch, scan_scratch_bytes(nT + 1)));
-  CK(scan_exclusive(ok, ok, nT + 1, nullptr, 0, nT + 1, c->scanScratch.p, dev_err(c), c->st, &c->launches, true));
+  CK(scan_exclusive(ok, ok, nT + 1, nullptr, 0, nT + 1, c->scanScratch.p, dev_err(c), c->st, &c->launches, true,
+                    c->wait));
   // 2. rows ordered by layer triplet, then by event (segment order inside a layer triplet)
   std::vector<uint32_t> cnt(S);
   if (S) CK(cudaMemcpyAsync(cnt.data(), c->fitSegCnt.p, (size_t)S * 4, cudaMemcpyDeviceToHost, c->st));

@@ -284,6 +284,29 @@ __global__ void ca_level_kernel(DevConfig cfg, uint32_t level, const uint32_t* _
   }
 }
 
+// The reference's forward iteration over any link set (`iteration`,
+// CellularAutomaton.h:52-100): next[f] = max(next[f], cur[f] + (cur[b] ==
+// cur[f])) for every link b -> f, and a living flag when a follower's state
+// equals its basis's.  The host repeats it, swapping the buffers without
+// copying (CellularAutomaton.cpp:52-98), until no cell lives.  Used for
+// caller-provided links, which need not go from one layer triplet to the
+// next as the chain's own do.
+__global__ void ca_iteration_kernel(const uint32_t* __restrict__ basis, const uint32_t* __restrict__ follower,
+                                    uint32_t nLinks, const uint32_t* __restrict__ cur, uint32_t* next,
+                                    uint32_t* living) {
+  GRID_STRIDE(p, nLinks) {
+    const uint32_t f = follower[p];
+    const uint32_t fs = cur[f];
+    const uint32_t same = cur[basis[p]] == fs ? 1u : 0u;
+    atomicMax(&next[f], fs + same);
+    if (same) *living = 1u;
+  }
+}
+
+__global__ void fill_u32_kernel(uint32_t* p, uint32_t v, uint32_t n) {
+  GRID_STRIDE(i, n) p[i] = v;
+}
+
 // followerBestBasisStore semantics (CellularAutomaton.h:212-263)
 __global__ void ca_best_kernel(const float* __restrict__ pt,
                                const uint32_t* __restrict__ inStart, const uint32_t* __restrict__ inList,
@@ -436,6 +459,21 @@ cudaError_t ca_forward(const DevConfig& cfg, CABuffers b, const uint32_t* nTDev,
     ca_level_kernel<<<grid_for(maxT, 256), 256, 0, st>>>(cfg, level, b.segOf, b.inStart, b.inList, nTDev, b.states);
     if (launches) *launches += 1;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t ca_iteration(const uint32_t* basis, const uint32_t* follower, uint32_t nLinks, const uint32_t* cur,
+                         uint32_t* next, uint32_t* living, cudaStream_t st, uint32_t* launches) {
+  if (nLinks == 0) return cudaSuccess;
+  ca_iteration_kernel<<<grid_for(nLinks, 256), 256, 0, st>>>(basis, follower, nLinks, cur, next, living);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t fill_u32(uint32_t* p, uint32_t v, uint32_t n, cudaStream_t st, uint32_t* launches) {
+  if (n == 0) return cudaSuccess;
+  fill_u32_kernel<<<grid_for(n, 256), 256, 0, st>>>(p, v, n);
+  if (launches) *launches += 1;
   return cudaGetLastError();
 }
 

@@ -22,7 +22,8 @@ constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __global__ void __launch_bounds__(SCAN_THREADS)
     scan_kernel(const uint32_t* __restrict__ in, uint32_t* out, uint64_t nHost, const uint32_t* nDev,
-                uint32_t nAdd, unsigned long long* status, uint32_t* ticket, uint32_t* err, uint32_t overflowBit) {
+                uint32_t nAdd, unsigned long long* status, uint32_t* ticket, uint32_t* err, uint32_t overflowBit,
+                WaitCtl ctl) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_warp[SCAN_THREADS / 32];
   __shared__ unsigned long long s_wide[SCAN_THREADS / 32];
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(SCAN_THREADS)
     agg = __shfl_sync(0xffffffffu, agg, 0);
     // publish and look back (bounded waits); the 32-bit outputs wrap like the
     // reference's uint scan, the exact total flags a count past 2^32
-    const unsigned long long excl = lb_exclusive_prefix(status, tile, agg, err);
+    const unsigned long long excl = lb_exclusive_prefix(status, tile, agg, err, ctl);
     if (lane == 0) {
       s_prefix = (uint32_t)excl;
       if (overflowBit && excl + agg > 0xffffffffull) raise_error(err, overflowBit);
@@ -172,7 +173,7 @@ size_t scan_scratch_bytes(uint64_t maxN) {
 
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const uint32_t* nDev, uint32_t nAdd,
                            uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches,
-                           bool flagOverflow) {
+                           bool flagOverflow, WaitCtl ctl) {
   uint64_t cap = nDev ? maxN : n;
   if (cap == 0) return cudaSuccess;
   uint64_t tiles = (cap + SCAN_TILE - 1) / SCAN_TILE;
@@ -182,7 +183,7 @@ cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const 
   uint32_t* ticket = reinterpret_cast<uint32_t*>(scratch);
   unsigned long long* status = reinterpret_cast<unsigned long long*>(static_cast<char*>(scratch) + 256);
   scan_kernel<<<(unsigned)tiles, SCAN_THREADS, 0, st>>>(in, out, n, nDev, nAdd, status, ticket, err,
-                                                        flagOverflow ? TRAX_EBIT_OVERFLOW : 0u);
+                                                        flagOverflow ? TRAX_EBIT_OVERFLOW : 0u, ctl);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }
@@ -208,8 +209,8 @@ cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint
 // process exits.  All calls share it: each call clears the part it uses
 // before its kernel runs, and two calls whose work overlaps on the GPU (on
 // different streams, or from different host threads) race on it.
+#include <atomic>
 #include <cstdio>
-#include <mutex>
 
 #include "trax/trax.h"
 
@@ -221,9 +222,15 @@ constexpr size_t NOALLOC_BYTES = NOALLOC_HEADER + NOALLOC_TILES * sizeof(unsigne
 
 static __device__ __align__(256) unsigned char g_noalloc_scan_scratch[NOALLOC_BYTES];
 
-constexpr int NOALLOC_MAX_DEVICES = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+// The no-alloc scan's wait settings (trax_noalloc_set_wait), process-wide.
+std::atomic<uint32_t> g_noalloc_spin{0}, g_noalloc_skip{0xffffffffu};
+
+trax::WaitCtl noalloc_wait() {
+  trax::WaitCtl w;
+  w.spinLimit = g_noalloc_spin.load();
+  w.skipTile = g_noalloc_skip.load();
+  return w;
+}
 
 void noalloc_msg(char* buf, size_t len, const char* msg) {
   if (buf && len) {
@@ -248,27 +255,20 @@ extern "C" int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, ui
     noalloc_msg(err_msg, err_len, b);
     return TRAX_ERR_ARG;
   }
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) {
-    noalloc_msg(err_msg, err_len, "trax_prefix_sum_noalloc: no usable current device");
-    return TRAX_ERR_CUDA;
-  }
+  // The array's device address, looked up on every call: an address belongs
+  // to a CUDA context, not to a device, so a cached one would be wrong after
+  // the caller resets the device or makes another context current.  Host code
+  // may not use the symbol itself as a device pointer.  The lookup is cheap
+  // next to the stream synchronisation below; the first one in a context also
+  // loads this library's device code there.
   void* base = nullptr;
-  {
-    // first call on this device: look up the device address of the array
-    // (host code may not use the symbol itself as a device pointer)
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scan_scratch);
-      if (e != cudaSuccess || !p) {
-        noalloc_msg(err_msg, err_len, "trax_prefix_sum_noalloc: cudaGetSymbolAddress failed");
-        return TRAX_ERR_CUDA;
-      }
-      g_noalloc_addr[dev] = p;
-    }
-    base = g_noalloc_addr[dev];
+  cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_scan_scratch);
+  if (e != cudaSuccess || !base) {
+    char b[200];
+    snprintf(b, sizeof b, "trax_prefix_sum_noalloc: cudaGetSymbolAddress failed (%s)",
+             e != cudaSuccess ? cudaGetErrorString(e) : "null address");
+    noalloc_msg(err_msg, err_len, b);
+    return TRAX_ERR_CUDA;
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const uint64_t tiles = (n + trax::SCAN_TILE - 1) / trax::SCAN_TILE;
@@ -279,7 +279,7 @@ extern "C" int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, ui
   e = cudaMemsetAsync(base, 0, NOALLOC_HEADER + tiles * sizeof(unsigned long long), st);
   if (e == cudaSuccess) {
     trax::scan_kernel<<<(unsigned)tiles, trax::SCAN_THREADS, 0, st>>>(d_in, d_out, n, nullptr, 0, status, ticket,
-                                                                      err, 0u);
+                                                                      err, 0u, noalloc_wait());
     e = cudaGetLastError();
   }
   uint32_t hostErr = 0;
@@ -293,5 +293,11 @@ extern "C" int trax_prefix_sum_noalloc(const uint32_t* d_in, uint32_t* d_out, ui
     noalloc_msg(err_msg, err_len, "trax_prefix_sum_noalloc: a bounded look-back wait ran out");
     return TRAX_ERR_TIMEOUT;
   }
+  return TRAX_OK;
+}
+
+extern "C" int trax_noalloc_set_wait(uint32_t polls, uint32_t skip_tile) {
+  g_noalloc_spin.store(polls);
+  g_noalloc_skip.store(skip_tile);
   return TRAX_OK;
 }

@@ -76,4 +76,13 @@ __device__ __forceinline__ uint32_t cell_at(const uint32_t* lGrid, uint32_t k, u
 // up, records TRAX_EBIT_TIMEOUT and carries on with what it has.
 #define TRAX_SPIN_LIMIT (1u << 22)
 
+// Settings of the scans' bounded waits, passed to every scan launch:
+// spinLimit polls before a wait gives up (0: TRAX_SPIN_LIMIT), and a tile
+// that publishes nothing (0xffffffff: none) -- a host-set fault that makes
+// its successors' waits run out, for testing the timeout path.
+struct WaitCtl {
+  uint32_t spinLimit = 0;
+  uint32_t skipTile = 0xffffffffu;
+};
+
 }  // namespace trax

@@ -17,10 +17,11 @@ namespace trax {
 size_t scan_scratch_bytes(uint64_t maxN);
 // Exclusive scan of n elements (or *nDev + nAdd when nDev != nullptr, with
 // maxN bounding the launch), in place allowed.  Outputs wrap modulo 2^32;
-// with flagOverflow a total of 2^32 or more sets TRAX_EBIT_OVERFLOW.
+// with flagOverflow a total of 2^32 or more sets TRAX_EBIT_OVERFLOW.  `ctl`
+// bounds the look-back waits (and may name a tile that never publishes).
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, const uint32_t* nDev, uint32_t nAdd,
                            uint64_t maxN, void* scratch, uint32_t* err, cudaStream_t st, uint32_t* launches,
-                           bool flagOverflow);
+                           bool flagOverflow, WaitCtl ctl);
 cudaError_t max_scan_inclusive(uint32_t* data, uint32_t n, cudaStream_t st, uint32_t* launches);
 
 // ------------------------------------------------------ event bucketing
@@ -239,6 +240,11 @@ cudaError_t ca_fill(const uint32_t* basis, const uint32_t* follower, const uint3
                     CABuffers b, const uint32_t* nTDev, uint64_t maxT, cudaStream_t st, uint32_t* launches);
 cudaError_t ca_forward(const DevConfig& cfg, CABuffers b, const uint32_t* nTDev, uint64_t maxT, cudaStream_t st,
                        uint32_t* launches);
+// One forward iteration of the reference's CA over any link set
+// (CellularAutomaton.h:52-100); *living is set when a cell lives.
+cudaError_t ca_iteration(const uint32_t* basis, const uint32_t* follower, uint32_t nLinks, const uint32_t* cur,
+                         uint32_t* next, uint32_t* living, cudaStream_t st, uint32_t* launches);
+cudaError_t fill_u32(uint32_t* p, uint32_t v, uint32_t n, cudaStream_t st, uint32_t* launches);
 cudaError_t ca_backward(const float* pt, CABuffers b, const uint32_t* nTDev, uint64_t maxT,
                         const uint32_t* nLinksDev, cudaStream_t st, uint32_t* launches);
 cudaError_t ca_tracks(CABuffers b, const uint32_t* nTDev, uint64_t maxT, uint32_t* tracks, uint64_t maxTracks,

@@ -5,9 +5,9 @@
 // 1 = tile aggregate, 2 = inclusive prefix) and a 62-bit value, so that sums
 // past 2^32 stay exact and a 32-bit overflow can be detected.  Warp 0 of a
 // tile reads 32 predecessors at a time until it meets an inclusive prefix.
-// The wait for a predecessor is bounded: after TRAX_SPIN_LIMIT polls the tile
-// records TRAX_EBIT_TIMEOUT, counts the missing predecessors as empty and
-// finishes, so a lost tile can never hang the GPU.
+// The wait for a predecessor is bounded: after TRAX_SPIN_LIMIT polls (or the
+// caller's limit) the tile records TRAX_EBIT_TIMEOUT, counts the missing
+// predecessors as empty and finishes, so a lost tile can never hang the GPU.
 #pragma once
 
 #include "trax_device.cuh"
@@ -31,16 +31,20 @@ __device__ __forceinline__ void lb_store(unsigned long long* p, unsigned long lo
 
 // Called by all 32 lanes of ONE warp with the tile's aggregate; returns (in
 // every lane) the sum of all earlier tiles and publishes this tile's
-// inclusive prefix.
+// inclusive prefix.  `ctl` bounds the waits and names a tile that publishes
+// nothing (a test fault).
 __device__ __forceinline__ unsigned long long lb_exclusive_prefix(unsigned long long* status, uint32_t tile,
-                                                                  unsigned long long agg, uint32_t* err) {
+                                                                  unsigned long long agg, uint32_t* err,
+                                                                  WaitCtl ctl) {
   const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t limit = ctl.spinLimit ? ctl.spinLimit : TRAX_SPIN_LIMIT;
+  const bool publish = tile != ctl.skipTile;
   agg &= LB_VALUE_MASK;
   if (tile == 0) {
-    if (lane == 0) lb_store(&status[0], LB_FLAG_PREFIX | agg);
+    if (lane == 0 && publish) lb_store(&status[0], LB_FLAG_PREFIX | agg);
     return 0ull;
   }
-  if (lane == 0) lb_store(&status[tile], LB_FLAG_AGG | agg);
+  if (lane == 0 && publish) lb_store(&status[tile], LB_FLAG_AGG | agg);
   unsigned long long excl = 0;
   int64_t pred = (int64_t)tile - 1;
   uint32_t spins = 0;
@@ -49,7 +53,7 @@ __device__ __forceinline__ unsigned long long lb_exclusive_prefix(unsigned long 
     unsigned long long s = (idx >= 0) ? lb_load(&status[idx]) : (LB_FLAG_PREFIX | 0ull);
     unsigned long long flag = s & LB_FLAG_MASK;
     if (__any_sync(0xffffffffu, flag == 0ull)) {
-      if (++spins < TRAX_SPIN_LIMIT) {
+      if (++spins < limit) {
         __nanosleep(64);
         continue;
       }
@@ -70,7 +74,7 @@ __device__ __forceinline__ unsigned long long lb_exclusive_prefix(unsigned long 
     if (pmask) break;
     pred -= 32;
   }
-  if (lane == 0) lb_store(&status[tile], LB_FLAG_PREFIX | ((excl + agg) & LB_VALUE_MASK));
+  if (lane == 0 && publish) lb_store(&status[tile], LB_FLAG_PREFIX | ((excl + agg) & LB_VALUE_MASK));
   return excl;
 }
 
