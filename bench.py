@@ -17,15 +17,22 @@ plain      the per-event launch structure of the reference (one event per
            stage call, host-synced count/scan/store) over the first events
 roofline   the dominant kernel's algorithmic bytes / its CUDA-event time
            against the measured HBM copy bandwidth
-cpu_baseline  the CPU oracle (a restatement of the reference kernels; the
-           reference's OpenCL build cannot run here) on a bounded sample
+cpu_baseline  the reference's own OpenCL kernel text compiled for the CPU
+           (oracle/_ref, built where the reference's sources were available;
+           "kind": "reference"), else the CPU oracle that restates it
+           ("kind": "port"), on a bounded sample on all host cores
+parity     every event of the batch against the oracle run on it alone
+
+Both arms run the workload's grid (250 x 48, the autotuner's grid choice for
+this workload on GB300); the GPU arm autotunes its block sizes live, and
+searches the grid too with --tune-grid.
 
 Multi-GPU (torchrun): every rank processes its own 1000-event batch on its
 own GPU (events are independent; no collective on the data path); value is
 all ranks' events over the slowest rank's time.
 
---impl reference times the CPU restatement of the reference on the host
-cores instead (rank 0 only).
+--impl reference times the reference's CPU path on the host cores instead
+(rank 0 only): oracle/_ref when built, else the oracle port.
 """
 from __future__ import annotations
 
@@ -69,6 +76,8 @@ def parse():
     p.add_argument("--runtime-csv", default=None, help="write the timed steps as the reference's runtime csv")
     p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: autotuned)")
     p.add_argument("--no-tune", action="store_true", help="skip the autotuner (grid of the workload, default blocks)")
+    p.add_argument("--tune-grid", action="store_true",
+                   help="let the autotuner search the grid too (the reference arm keeps the workload's grid)")
     p.add_argument("--tune-cache", default=None, help="JSON cache file of the autotuner")
     p.add_argument("--blocks", default=None,
                    help="block sizes of the pair, prediction and filter kernels, e.g. 256,64,256 (skips their tuning)")
@@ -133,17 +142,44 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_baseline(batch, n_events: int):
+def cpu_engine():
+    """The reference's CPU path to time: its own kernel text compiled for the
+    CPU (oracle/_ref) when that was built, else the oracle port."""
+    from oracle import ref
+    if ref.available():
+        return "reference"
+    return "port"
+
+
+def cpu_run(sample, cores: int, kind: str) -> int:
+    """Runs the CPU path over `sample`, one event per group on `cores` host
+    threads; returns the number of triplets."""
+    if kind == "reference":
+        from oracle import ref
+        return int(ref.run_events(sample, workers=cores).sum())
     from oracle import oracle
+    res = oracle.run(sample, event_grouping=1, n_workers=cores, arrays=("stats",))
+    return sum(r["stats_dict"]["triplets"] for r in res)
+
+
+CPU_KIND_NOTE = {
+    "reference": "the reference's own OpenCL kernel text (src/algorithms/*.h KERNEL_CLASS blocks) compiled for the "
+                 "CPU against a work-item shim, driven by its host sequences; exec.threads 1, a 32 KB CPU device",
+    "port": "the oracle's restatement of the reference kernels (the reference's kernel text was not built here)",
+}
+
+
+def cpu_baseline(batch, n_events: int):
     sample = batch.subset(range(min(n_events, batch.n_events)))
     cores = os.cpu_count() or 1
+    kind = cpu_engine()
     t0 = time.perf_counter()
-    res = oracle.run(sample, event_grouping=1, n_workers=cores, arrays=("stats",))
+    trip = cpu_run(sample, cores, kind)
     dt = time.perf_counter() - t0
-    trip = sum(r["stats_dict"]["triplets"] for r in res)
-    return {"value": round(sample.n_events / dt, 3), "unit": "events/s", "cores": cores, "kind": "port",
-            "sample": f"first {sample.n_events} events of the 1000-event workload, one event per group, "
-                      f"{cores} host threads, {dt:.2f} s wall",
+    return {"value": round(sample.n_events / dt, 3), "unit": "events/s", "cores": cores, "kind": kind,
+            "sample": f"first {sample.n_events} events of the 1000-event workload at the same grid "
+                      f"({batch.n_z}x{batch.n_phi}), one event per group, {cores} host threads, {dt:.2f} s wall; "
+                      + CPU_KIND_NOTE[kind],
             "triplets_per_s": round(trip / dt, 1)}
 
 
@@ -261,16 +297,67 @@ def run_plain(ctx, batch, n_events):
             "structure": "one event per stage call; host-synced count -> scan -> read total -> store"}
 
 
-def parity_sample(ctx, batch, n=6):
-    from oracle import oracle
-    sub = batch.subset(range(n))
-    ref = oracle.run(sub)[0]
-    ctx.upload(sub)
+class WholeBatchOracle:
+    """The oracle on the whole batch as one event group, in a background host
+    thread (the call releases the GIL): links, connectable lists, pt and the
+    CA depend on the events grouped together, so they are checked against
+    this run, not against events run alone."""
+
+    def __init__(self, batch):
+        self.result, self.error, self.wall = None, None, 0.0
+        self.thread = threading.Thread(target=self._run, args=(batch,), daemon=True)
+        self.thread.start()
+
+    def _run(self, batch):
+        from oracle import oracle
+        t0 = time.perf_counter()
+        try:
+            self.result = oracle.run(batch)[0]
+        except Exception as exc:  # reported by parity_full
+            self.error = exc
+        self.wall = time.perf_counter() - t0
+
+    def get(self):
+        self.thread.join()
+        if self.error is not None:
+            raise self.error
+        return self.result
+
+
+def parity_full(ctx, batch, whole):
+    """The batched results of the full batch against the oracle: every event's
+    slice of pairs, candidates, triplets and eta against the event run alone,
+    and every array against the whole batch run as one group
+    (oracle/batch_slices.py)."""
+    from oracle import batch_slices, oracle
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    refs = oracle.run(batch, event_grouping=1, n_workers=cores,
+                      arrays=("pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "eta"))
+    ctx.upload(batch)
     ctx.seed_batch(use_graph=True)
-    got = ctx.results()
-    ok = all(np.array_equal(np.asarray(got[k]), np.asarray(ref[k]))
-             for k in ("pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "link_basis", "link_follower", "tracks"))
-    return f"{'bit-exact' if ok else 'MISMATCH'} against the CPU oracle on the first {n} events"
+    got = {}
+    p, got["pair_offsets"] = ctx.pairs()
+    got["pairs"] = p.reshape(-1)
+    c, got["cand_offsets"] = ctx.candidates()
+    got["cands"] = c.reshape(-1)
+    got["trip_h1"], got["trip_h2"], got["trip_h3"], got["trip_offsets"] = ctx.triplets()
+    got["eta"], got["pt"] = ctx.eta_pt()
+    (got["link_basis"], got["link_follower"], got["connectable"],
+     got["non_connectable"]) = ctx.links()
+    got["ca_states"], got["tracks"], got["track_offsets"] = ctx.tracks()
+    per_event = batch_slices.compare(batch, got, refs)
+    t_events = time.perf_counter() - t0
+    diff = batch_slices.compare_whole(got, whole.get())
+    ok = not per_event["mismatch"] and not diff
+    return {"result": "bit-exact" if ok else "MISMATCH",
+            "events": per_event["events"], "per_event_mismatch": per_event["mismatch"],
+            "whole_batch_mismatch": diff,
+            "checked": "every event's slice of pairs, candidates, triplet hits and eta bits against the CPU "
+                       "oracle run on the event alone (16 host threads); all arrays -- also links, "
+                       "connectable lists, pt, CA states, best bases and tracks -- against the oracle run on "
+                       "the whole batch as one event group",
+            "oracle_wall_s": {"events_alone": round(t_events, 2), "whole_batch": round(whole.wall, 2)}}
 
 
 def run_alignment(device: int):
@@ -328,8 +415,8 @@ def run_ours(args, ranks):
     if args.blocks:
         ctx.set_block_sizes(*(int(v) for v in args.blocks.split(",")))
     elif not args.no_tune:
-        # grid searched unless --grid fixes it; block sizes always
-        tune = ctx.autotune(cache_path=args.tune_cache, search_grid=not args.grid)
+        # block sizes always; the grid only with --tune-grid
+        tune = ctx.autotune(cache_path=args.tune_cache, search_grid=bool(args.tune_grid and not args.grid))
         batch.n_z, batch.n_phi = tune["n_z"], tune["n_phi"]
     shape = ctx.launch_config()
     cells = batch.n_events * batch.n_layers * (batch.n_z + 1) * (batch.n_phi + 1)
@@ -362,6 +449,8 @@ def run_ours(args, ranks):
         with open(args.runtime_csv, "w") as f:
             f.write(records.csv())
     clk = clocks.stop()
+    # the oracle on the whole batch, on one host thread while the rest runs
+    whole = WholeBatchOracle(batch) if (ranks.rank == 0 and not args.no_parity) else None
     ranks.barrier()
     my_time = sum(dev_ms) / 1e3
     t_max = ranks.max(my_time)
@@ -524,7 +613,7 @@ def run_ours(args, ranks):
             result["plain_per_event"] = plain
             result["batched_over_plain"] = round(value / ranks.world / plain["value"], 2)
         if not args.no_parity:
-            result["parity"] = parity_sample(ctx, batch)
+            result["parity"] = parity_full(ctx, batch, whole)
         if not args.no_cpu:
             result["cpu_baseline"] = cpu_baseline(batch, args.cpu_sample)
         if not args.no_align:
@@ -536,25 +625,26 @@ def run_ours(args, ranks):
 def run_reference(args, ranks):
     if ranks.rank != 0:
         return None
-    from oracle import oracle
     from trax_gb300 import events
     batch = events.generate(CONFIG, n_events=args.events)
+    if args.grid:
+        batch.n_z, batch.n_phi = (int(v) for v in args.grid.lower().split("x"))
     cores = os.cpu_count() or 1
-    # 8 events per host thread per step, so that the threads stay busy to the
+    kind = cpu_engine()
+    # 4 events per host thread per step, so that the threads stay busy to the
     # end of a step despite the spread of event sizes
-    per_step = min(max(8 * cores, 32), batch.n_events)
-    warm = batch.subset(range(min(8, batch.n_events)))
+    per_step = min(max(4 * cores, 32), batch.n_events)
+    warm = batch.subset(range(min(cores, batch.n_events)))
     for _ in range(max(args.warmup, 3)):
-        oracle.run(warm, event_grouping=1, n_workers=cores, arrays=("stats",))
+        cpu_run(warm, cores, kind)
     times, evs, trip = [], 0, 0
     for k in range(args.steps):
         lo = (k * per_step) % max(1, batch.n_events - per_step)
         sample = batch.subset(range(lo, lo + per_step))
         t0 = time.perf_counter()
-        res = oracle.run(sample, event_grouping=1, n_workers=cores, arrays=("stats",))
+        trip += cpu_run(sample, cores, kind)
         times.append(time.perf_counter() - t0)
         evs += sample.n_events
-        trip += sum(r["stats_dict"]["triplets"] for r in res)
     total = sum(times)
     v = round(evs / total, 3)
     return {
@@ -562,12 +652,13 @@ def run_reference(args, ranks):
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * total / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "ttbar-like batch: 1000 events, tracks ~ Poisson(U[300,3000]), 10 layers, 6 layer "
-                               "triplets, seed 2 (config 2)", "events_per_step": per_step},
+                               "triplets, seed 2 (config 2)", "events_per_step": per_step,
+                   "grid": f"{batch.n_z}x{batch.n_phi}"},
         "triplets_per_s": round(trip / total, 1),
-        "cpu_baseline": {"value": v, "unit": "events/s", "cores": cores, "kind": "port",
-                         "sample": f"{per_step} events per step of the 1000-event workload, one event per group; "
-                                   "CPU restatement of the reference kernels (the reference's OpenCL build "
-                                   "cannot run: empty clever submodule, no OpenCL ICD)"},
+        "cpu_baseline": {"value": v, "unit": "events/s", "cores": cores, "kind": kind,
+                         "sample": f"{per_step} events per step of the 1000-event workload (rotating windows) at "
+                                   f"grid {batch.n_z}x{batch.n_phi}, one event per group, {cores} host threads; "
+                                   + CPU_KIND_NOTE[kind]},
         "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

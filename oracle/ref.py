@@ -27,6 +27,8 @@ ARRAYS = ["hx", "hy", "hz", "hlayer", "hdet", "hhit", "hevt", "grid", "pairs", "
 # A GTX 660's local memory (the reference's published GPU); 0 selects the
 # no-local-memory kernel variants.
 GTX660_LOCAL_MEM = 48 * 1024
+# The local memory an OpenCL CPU device reports (32 KB on Intel's runtime).
+CPU_LOCAL_MEM = 32 * 1024
 
 _lock = threading.Lock()
 _lib = None
@@ -66,6 +68,9 @@ def lib():
             L.ref_ca.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
                                  ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
             L.ref_ca.restype = ctypes.c_int
+            L.ref_run_events.argtypes = [ctypes.POINTER(oracle._Input), ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.c_uint32, ctypes.c_void_p]
+            L.ref_run_events.restype = ctypes.c_int
             _lib = L
         return _lib
 
@@ -120,6 +125,17 @@ def ca(n_triplets: int, basis, follower, pt, n_threads: int = 1, max_ca_iteratio
         return out
     finally:
         L.ref_free(h)
+
+
+def run_events(batch, workers: int, n_threads: int = 1, local_mem: int = CPU_LOCAL_MEM) -> np.ndarray:
+    """The reference's kernels over every event of `batch`, each event its own
+    group, on `workers` host threads; returns the triplet count of each event."""
+    L = lib()
+    inp, keep = oracle.make_input(batch)
+    out = np.zeros(batch.n_events, dtype=np.uint64)
+    if L.ref_run_events(ctypes.byref(inp), n_threads, local_mem, workers, out.ctypes.data) != 0:
+        raise RuntimeError(L.ref_last_error().decode())
+    return out
 
 
 def prefix_sum(data: np.ndarray, wg: int) -> np.ndarray:

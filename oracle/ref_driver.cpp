@@ -40,11 +40,13 @@
 #include <ucontext.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <functional>
 #include <limits>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ref_kernels.cpp"
@@ -817,6 +819,55 @@ int ref_ca(uint32_t n_triplets, const uint32_t* basis, const uint32_t* follower,
                 R.st.ca_chain_broken, R.st.grid_count_local, R.st.grid_store_variant, R.st.pair_count_local};
   *out = res;
   return 0;
+}
+
+// The reference's CPU path over many events: each event is its own event
+// group (the reference's eventGrouping = 1) and the groups run on `workers`
+// host threads.  Only the triplet count of each event is returned (in
+// triplets[e]); this is what the CPU baseline times.  Returns 0, or -1 on
+// invalid input.
+int ref_run_events(const oracle_input* in, uint32_t n_threads, uint32_t local_mem_bytes, uint32_t workers,
+                   uint64_t* triplets) {
+  if (!in || in->n_events == 0 || n_threads == 0) {
+    g_error = "invalid input";
+    return -1;
+  }
+  const uint32_t E = in->n_events, L = in->n_layers;
+  std::atomic<uint32_t> next{0};
+  std::atomic<int> failed{0};
+  auto work = [&] {
+    for (uint32_t e = next++; e < E; e = next++) {
+      const uint32_t first = in->event_offsets[e];
+      const uint32_t last = e + 1 < E ? in->event_offsets[e + 1] : in->n_hits;
+      oracle_input one = *in;
+      std::vector<uint32_t> evt(last - first, 0u);
+      const uint32_t zero = 0;
+      one.n_hits = last - first;
+      one.x = in->x + first;
+      one.y = in->y + first;
+      one.z = in->z + first;
+      one.layer = in->layer + first;
+      one.det_id = in->det_id + first;
+      one.hit_id = in->hit_id + first;
+      one.event = evt.data();
+      one.n_events = 1;
+      one.event_offsets = &zero;
+      one.layer_hits = in->layer_hits + (size_t)e * L;
+      one.layer_offsets = in->layer_offsets + (size_t)e * L;
+      ref_result* r = nullptr;
+      if (ref_run(&one, n_threads, local_mem_bytes, 100000, &r) != 0) {
+        failed = 1;
+        return;
+      }
+      triplets[e] = r->arrays["trip_h1"].size();
+      delete r;
+    }
+  };
+  std::vector<std::thread> pool;
+  for (uint32_t w = 1; w < std::max(workers, 1u); ++w) pool.emplace_back(work);
+  work();
+  for (auto& t : pool) t.join();
+  return failed ? -1 : 0;
 }
 
 const char* ref_last_error(void) { return g_error.c_str(); }

@@ -108,39 +108,31 @@ def test_warp_tile_boundaries(ctx, oracle_lib):
 
 
 def test_full_batch_equals_its_events_run_alone(ctx, oracle_lib):
-    """At the benchmark's full size (1000 events, 9.7 M hits): events are
-    independent, so each event's slice of the batched results equals the
-    oracle's results for that event alone, hit indices shifted by the event's
-    first hit and pair indices by its first pair.  Twelve events are checked
-    that way; over the whole batch the triplet offsets are monotone and every
-    segment's triplets are sorted by (h2, h1) (non-decreasing: a pair can
-    have several third hits)."""
+    """At the benchmark's full size (1000 events, 9.7 M hits): every event's
+    slice of the batched pairs, candidates, triplets and eta equals the
+    oracle's results for that event alone, indices shifted by the event's
+    first hit and pair (oracle/batch_slices.py), and every array -- links,
+    connectable lists, pt and the CA included, which depend on the events
+    grouped together -- equals the oracle run on the whole batch as one
+    group.  The triplet offsets are monotone and every segment's triplets are
+    sorted by (h2, h1) (non-decreasing: a pair can have several third
+    hits)."""
+    import os
+    from oracle import batch_slices
     batch = events.generate(2)
     ctx.upload(batch)
     ctx.seed_batch(use_graph=True)
     got = ctx.results()
-    n_lt = len(batch.lts)
-    sentinel = np.uint32(0xFFFFFFFF)
-    po, co, to = (np.asarray(got[k]) for k in ("pair_offsets", "cand_offsets", "trip_offsets"))
-    hits_per_event = np.diff(np.append(batch.event_offsets, batch.n_hits))
-    rng = np.random.default_rng(0)
-    small = np.nonzero(hits_per_event[:-1] < 8000)[0]
-    sample = sorted(set(rng.choice(small, 10, replace=False).tolist()) | {0, batch.n_events - 2})
-    for e in sample:
-        ref = oracle_lib.run(batch.subset([e]))[0]
-        off = np.uint32(batch.event_offsets[e])
-        pa, pb = int(po[e * n_lt]), int(po[(e + 1) * n_lt])
-        pairs = np.asarray(got["pairs"])[2 * pa:2 * pb].copy()
-        pairs[pairs != sentinel] -= off
-        assert np.array_equal(pairs, ref["pairs"]), e
-        ca, cb = int(co[e * n_lt]), int(co[(e + 1) * n_lt])
-        cands = np.asarray(got["cands"])[2 * ca:2 * cb].reshape(-1, 2).copy()
-        cands[:, 0] -= np.uint32(pa)
-        cands[cands[:, 1] != sentinel, 1] -= off
-        assert np.array_equal(cands.reshape(-1), ref["cands"]), e
-        ta, tb = int(to[e * n_lt]), int(to[(e + 1) * n_lt])
-        for k in ("trip_h1", "trip_h2", "trip_h3"):
-            assert np.array_equal(np.asarray(got[k])[ta:tb] - off, ref[k]), (e, k)
+    refs = oracle_lib.run(batch, event_grouping=1, n_workers=os.cpu_count() or 1,
+                          arrays=("pairs", "cands", "trip_h1", "trip_h2", "trip_h3", "eta"))
+    res = batch_slices.compare(batch, got, refs)
+    assert res["events"] == batch.n_events
+    assert not res["mismatch"], res["mismatch"]
+    # links, connectable lists, pt and the CA depend on the events grouped
+    # together: against the oracle on the whole batch as one group
+    whole = oracle_lib.run(batch)[0]
+    assert batch_slices.compare_whole(got, whole) == []
+    to = np.asarray(got["trip_offsets"])
     assert np.all(np.diff(to.astype(np.int64)) >= 0)
     h1, h2 = (np.asarray(got[k]).astype(np.uint64) for k in ("trip_h1", "trip_h2"))
     key = (h2 << np.uint64(32)) | h1

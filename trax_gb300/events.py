@@ -133,11 +133,15 @@ def workload(config: int, n_events: Optional[int] = None) -> Workload:
     elif config in (2, 4):
         # the alignment workload adds the layer triplets (7,8,9) and (8,9,10):
         # with only the first six, layers 9 and 10 are in no triplet and
-        # their shifts have no gradient
+        # their shifts have no gradient.  The ttbar-like workload's grid,
+        # 250 x 48, is trax_autotune's choice for it on a GB300 (a search
+        # over 35 grids: 200 x 64, 300 x 48 and 150 x 64 within 1 %); every
+        # implementation timed on this workload runs that grid.
+        nz, nphi = (250, 48) if config == 2 else (50, 128)
         w = Workload("ttbarlike-1000-uneven-10layer" if config == 2 else "alignment-1000-10layer",
                      config, 1000, BARREL10_RADII,
                      layer_triplets([1, 2, 3, 4, 5, 6] if config == 2 else [1, 2, 3, 4, 5, 6, 7, 8]),
-                     50, 128, 0.7, tracks="poisson_uniform_lambda", pt_dist="powerlaw3",
+                     nz, nphi, 0.7, tracks="poisson_uniform_lambda", pt_dist="powerlaw3",
                      pt_range=(0.7, 0.0), eta_max=2.5, misalign=(config == 4))
     elif config == 3:
         w = Workload("pileup-16x20x1000-10layer", 3, 16, BARREL10_RADII,
