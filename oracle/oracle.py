@@ -72,8 +72,10 @@ class _Input(ctypes.Structure):
         ("min_r", ctypes.c_void_p), ("max_r", ctypes.c_void_p),
         ("d_eta_cut", ctypes.c_float),
         ("n_threads", ctypes.c_uint32), ("event_grouping", ctypes.c_uint32),
-        ("n_workers", ctypes.c_uint32),
+        ("n_workers", ctypes.c_uint32), ("links_mode", ctypes.c_uint32),
     ]
+
+LINKS_MODES = {"scan": 0, "indexed": 1, "none": 2}
 
 
 def lib():
@@ -111,7 +113,7 @@ class OracleError(RuntimeError):
     pass
 
 
-def make_input(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1):
+def make_input(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1, links: str = "scan"):
     """The oracle_input struct for an EventBatch, and the arrays it points into
     (keep them alive while the struct is used)."""
     keep = []
@@ -150,15 +152,20 @@ def make_input(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: in
     inp.min_r, inp.max_r = arr(batch.min_r, np.float32), arr(batch.max_r, np.float32)
     inp.d_eta_cut = batch.d_eta_cut
     inp.n_threads, inp.event_grouping, inp.n_workers = n_threads, event_grouping, n_workers
+    inp.links_mode = LINKS_MODES[links]
     return inp, keep
 
 
 def run(batch, n_threads: int = 0, event_grouping: int = 0, n_workers: int = 1,
-        arrays: Optional[Sequence[str]] = None) -> List[Dict[str, np.ndarray]]:
+        arrays: Optional[Sequence[str]] = None, links: str = "scan") -> List[Dict[str, np.ndarray]]:
     """Run the oracle over an EventBatch; one dict of arrays per event group (only
-    `arrays` and the stats when given, e.g. ("stats",) for timing runs)."""
+    `arrays` and the stats when given, e.g. ("stats",) for timing runs).
+    links: "scan" (the reference's connectivity scan), "indexed" (the same
+    result through an index, for very large events) or "none" (no linking).
+    n_workers host threads run groups in parallel or, with one group, work
+    inside it; the results do not depend on their number."""
     L = lib()
-    inp, keep = make_input(batch, n_threads, event_grouping, n_workers)
+    inp, keep = make_input(batch, n_threads, event_grouping, n_workers, links)
     h = ctypes.c_void_p()
     rc = L.oracle_run(ctypes.byref(inp), ctypes.byref(h))
     if rc != 0:

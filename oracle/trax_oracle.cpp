@@ -47,6 +47,8 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <unordered_map>
+#include <memory>
 #include <vector>
 
 #include "../trax_gb300/csrc/trax_math.h"
@@ -103,8 +105,34 @@ struct Hits {
   std::vector<uint> layer, det, hid, evt, orig;
 };
 
+// Runs f(begin, end, worker) over [0, n) in chunks of at least `grain` on
+// `workers` host threads.  Used only where every index writes its own
+// outputs (or the same value to a shared flag), so the results do not
+// depend on the number of threads.
+template <class F>
+void parallel_for(uint64_t n, uint workers, uint64_t grain, F&& f) {
+  if (workers <= 1 || n <= grain) {
+    if (n) f((uint64_t)0, n, 0u);
+    return;
+  }
+  const uint64_t chunk = std::max<uint64_t>(grain, n / ((uint64_t)workers * 16));
+  std::atomic<uint64_t> next(0);
+  auto run = [&](uint w) {
+    for (;;) {
+      const uint64_t b = next.fetch_add(chunk);
+      if (b >= n) break;
+      f(b, std::min(n, b + chunk), w);
+    }
+  };
+  std::vector<std::thread> th;
+  for (uint w = 1; w < workers; ++w) th.emplace_back(run, w);
+  run(0);
+  for (auto& t : th) t.join();
+}
+
 struct Ctx {
   const oracle_input* in;
+  uint workers = 1;  // host threads inside this event group
   uint E, L, nZ, nP, C, nLT;
   float minZ, sZ, minPhi, sP;
   float minRcurv;
@@ -187,13 +215,18 @@ struct PairOut {
 
 // PairGeneratorBeamspot.h:43-246 (pairCount) and 448-525 (pairStore) for all
 // (event, layer triplet) segments, emulating nThreads work-items per segment.
-void pair_gen(Ctx& c, const std::vector<uint>& grid, PairOut& po) {
+// One (event, layer triplet) segment: its pairs, positions counted from 0.
+struct SegmentPairs {
+  std::vector<uint> pairs;
+  uint64_t windowTests = 0;
+};
+
+void pair_segment(const Ctx& c, const std::vector<uint>& grid, uint e, uint p, SegmentPairs& po) {
   const oracle_input* in = c.in;
   const Hits& h = c.h;
-  po.offsets.assign((size_t)c.E * c.nLT + 1, 0u);
-  uint running = 0;  // exclusive prefix over all previous segments' threads
-  for (uint e = 0; e < c.E; ++e) {
-    for (uint p = 0; p < c.nLT; ++p) {
+  uint running = 0;  // exclusive prefix over this segment's threads
+  {
+    {
       uint layer = in->lt_layer2[p] - 1;
       const uint* lGrid2 = &grid[((size_t)e * c.L + layer) * c.C];
       uint layer2Offset = lGrid2[0];
@@ -296,10 +329,32 @@ void pair_gen(Ctx& c, const std::vector<uint>& grid, PairOut& po) {
             pos += valid;
           }
         }
-        if (t == T - 1) po.offsets[(size_t)e * c.nLT + p + 1] = nextThread;
       }
       // slots the store kernel never reached stay as written above (sentinel)
     }
+  }
+}
+
+// The segments on the group's threads, concatenated in (event, layer
+// triplet) order; pairOffsets[e * nLT + p + 1] is the running total after
+// each segment (pairStore's last thread writes it).
+void pair_gen(Ctx& c, const std::vector<uint>& grid, PairOut& po) {
+  const uint nSeg = c.E * c.nLT;
+  std::vector<SegmentPairs> seg(nSeg);
+  parallel_for(nSeg, c.workers, 1, [&](uint64_t b, uint64_t e, uint) {
+    for (uint64_t k = b; k < e; ++k) pair_segment(c, grid, (uint)(k / c.nLT), (uint)(k % c.nLT), seg[k]);
+  });
+  po.offsets.assign((size_t)nSeg + 1, 0u);
+  size_t total = 0;
+  for (uint k = 0; k < nSeg; ++k) total += seg[k].pairs.size();
+  po.pairs.reserve(total);
+  uint running = 0;
+  for (uint k = 0; k < nSeg; ++k) {
+    po.pairs.insert(po.pairs.end(), seg[k].pairs.begin(), seg[k].pairs.end());
+    running += (uint)(seg[k].pairs.size() / 2);
+    po.offsets[k + 1] = running;
+    po.windowTests += seg[k].windowTests;
+    std::vector<uint>().swap(seg[k].pairs);
   }
   for (size_t k = 0; k < po.pairs.size(); k += 2)
     if (po.pairs[k] == SENTINEL) {
@@ -410,25 +465,29 @@ uint predict_pair(Ctx& c, const std::vector<uint>& grid, const uint* pr, uint gi
 void predict(Ctx& c, const std::vector<uint>& grid, const PairOut& po, PredOut& pr) {
   uint nPairs = (uint)(po.pairs.size() / 2);
   std::vector<uint> prefix((size_t)nPairs + 1, 0u);
-  for (uint g = 0; g < nPairs; ++g) {
-    uint wrote;
-    prefix[g] = predict_pair(c, grid, &po.pairs[2 * (size_t)g], g, false, nullptr, 0, pr.windowTests,
-                             wrote);
-  }
+  std::vector<uint64_t> tests(c.workers, 0), truncated(c.workers, 0), undefinedSlots(c.workers, 0);
+  parallel_for(nPairs, c.workers, 4096, [&](uint64_t b, uint64_t e, uint w) {
+    for (uint g = (uint)b; g < (uint)e; ++g) {
+      uint wrote;
+      prefix[g] = predict_pair(c, grid, &po.pairs[2 * (size_t)g], g, false, nullptr, 0, tests[w], wrote);
+    }
+  });
+  for (uint64_t t : tests) pr.windowTests += t;
   exclusive_scan(prefix, prefix.size());
   uint total = prefix[nPairs];
   pr.cands.assign((size_t)total * 2, SENTINEL);
   pr.offsets.assign((size_t)c.E * c.nLT + 1, 0u);
-  uint64_t dummy = 0;
-  for (uint g = 0; g < nPairs; ++g) {
+  parallel_for(nPairs, c.workers, 4096, [&](uint64_t b, uint64_t e, uint w) {
+   uint64_t dummy = 0;
+   for (uint g = (uint)b; g < (uint)e; ++g) {
     uint pos = prefix[g], next = prefix[g + 1];
     uint wrote = 0;
     uint storeValid =
         predict_pair(c, grid, &po.pairs[2 * (size_t)g], g, true,
                      next > pos ? &pr.cands[2 * (size_t)pos] : nullptr, next - pos, dummy, wrote);
-    if (storeValid > next - pos) pr.truncated += storeValid - (next - pos);
+    if (storeValid > next - pos) truncated[w] += storeValid - (next - pos);
     if (wrote < next - pos) {
-      pr.undefinedSlots += (next - pos) - wrote;
+      undefinedSlots[w] += (next - pos) - wrote;
       for (uint k = pos + wrote; k < next; ++k) {
         pr.cands[2 * (size_t)k] = g;
         pr.cands[2 * (size_t)k + 1] = SENTINEL;
@@ -448,6 +507,11 @@ void predict(Ctx& c, const std::vector<uint>& grid, const PairOut& po, PredOut& 
     } else {
       pr.offsets[(size_t)event * c.nLT + layerTriplet + 1] = next;
     }
+   }
+  });
+  for (uint w = 0; w < c.workers; ++w) {
+    pr.truncated += truncated[w];
+    pr.undefinedSlots += undefinedSlots[w];
   }
   for (size_t k = 1; k < pr.offsets.size(); ++k)
     if (pr.offsets[k] == 0) pr.offsets[k] = pr.offsets[k - 1];
@@ -522,8 +586,11 @@ void filter(const Ctx& c, const PairOut& po, const PredOut& pr, FilterOut& fo) {
   uint nCand = (uint)(pr.cands.size() / 2);
   uint nWords = (nCand + 31) / 32;
   std::vector<uint> oracle(nWords, 0u);
-  for (uint gid = 0; gid < nCand; ++gid)
-    if (filter_one(c, po, &pr.cands[2 * (size_t)gid])) oracle[gid / 32] |= (1u << (gid % 32));
+  parallel_for(nWords, c.workers, 256, [&](uint64_t b, uint64_t e, uint) {  // words of 32 candidates
+    for (uint64_t g = b; g < e; ++g)
+      for (uint gid = (uint)g * 32; gid < std::min(nCand, (uint)g * 32 + 32); ++gid)
+        if (filter_one(c, po, &pr.cands[2 * (size_t)gid])) oracle[gid / 32] |= (1u << (gid % 32));
+  });
   std::vector<uint> prefix((size_t)nWords + 1, 0u);
   for (uint g = 0; g < nWords; ++g) {
     uint i = oracle[g];  // SWAR popcount (:173-176)
@@ -536,20 +603,22 @@ void filter(const Ctx& c, const PairOut& po, const PredOut& pr, FilterOut& fo) {
   fo.h1.assign(nFound, 0u);
   fo.h2.assign(nFound, 0u);
   fo.h3.assign(nFound, 0u);
-  for (uint g = 0; g < nWords; ++g) {
-    uint pos = prefix[g];
-    uint lOracle = oracle[g];
-    for (uint i = 0; i < 32; ++i) {
-      bool valid = (lOracle >> i) & 1u;
-      if (valid) {
-        const uint* cand = &pr.cands[2 * ((size_t)g * 32 + i)];
-        fo.h1[pos] = po.pairs[2 * (size_t)cand[0]];
-        fo.h2[pos] = po.pairs[2 * (size_t)cand[0] + 1];
-        fo.h3[pos] = cand[1];
+  parallel_for(nWords, c.workers, 4096, [&](uint64_t b, uint64_t e, uint) {
+    for (uint g = (uint)b; g < (uint)e; ++g) {
+      uint pos = prefix[g];
+      uint lOracle = oracle[g];
+      for (uint i = 0; i < 32; ++i) {
+        bool valid = (lOracle >> i) & 1u;
+        if (valid) {
+          const uint* cand = &pr.cands[2 * ((size_t)g * 32 + i)];
+          fo.h1[pos] = po.pairs[2 * (size_t)cand[0]];
+          fo.h2[pos] = po.pairs[2 * (size_t)cand[0] + 1];
+          fo.h3[pos] = cand[1];
+        }
+        pos += valid;
       }
-      pos += valid;
     }
-  }
+  });
   filter_offsets(c, fo);
 }
 
@@ -599,35 +668,74 @@ bool conn_range(const Ctx& c, const FilterOut& fo, uint t, uint& begin, uint& en
   return true;
 }
 
+// The followers of every basis, as the count and store kernels visit them:
+// the triplets i in the basis's search range [begin, end) whose (h1, h2) is
+// the basis's (h2, h3), in ascending i.  The linear scan of
+// TripletConnectivityTight.h:134-139 (links_mode 0), or a lookup in an index
+// of all triplets by (h1, h2) (links_mode 1) -- the same indices in the same
+// order, without the scan's quadratic cost on large segments.
+struct FollowerIndex {
+  std::unordered_map<uint64_t, std::vector<uint>> byPair;
+  explicit FollowerIndex(const FilterOut& fo) {
+    for (uint i = 0; i < (uint)fo.h1.size(); ++i)
+      byPair[((uint64_t)fo.h1[i] << 32) | fo.h2[i]].push_back(i);  // ascending i
+  }
+  template <class F>
+  void each(uint inner, uint outer, uint begin, uint end, F&& f) const {
+    auto it = byPair.find(((uint64_t)inner << 32) | outer);
+    if (it == byPair.end()) return;
+    const std::vector<uint>& v = it->second;
+    for (auto k = std::lower_bound(v.begin(), v.end(), begin); k != v.end() && *k < end; ++k) f(*k);
+  }
+};
+
 // TripletConnectivityTight::run (.cpp:5-475)
 void connectivity(const Ctx& c, const FilterOut& fo, ConnOut& co) {
   uint nT = (uint)fo.h1.size();
   co.eta.assign(nT, 0.0f);
-  for (uint t = 0; t < nT; ++t) {  // tripletEtaCalculatorStore (:47-79)
-    uint hi = fo.h1[t], ho = fo.h3[t];
-    float px = c.h.x[ho] - c.h.x[hi];
-    float py = c.h.y[ho] - c.h.y[hi];
-    float pz = c.h.z[ho] - c.h.z[hi];
-    float tt = div_(pz, sqrt_(px * px + py * py));
-    co.eta[t] = asinh_(tt);
-  }
+  parallel_for(nT, c.workers, 4096, [&](uint64_t b, uint64_t e, uint) {
+    for (uint t = (uint)b; t < (uint)e; ++t) {  // tripletEtaCalculatorStore (:47-79)
+      uint hi = fo.h1[t], ho = fo.h3[t];
+      float px = c.h.x[ho] - c.h.x[hi];
+      float py = c.h.y[ho] - c.h.y[hi];
+      float pz = c.h.z[ho] - c.h.z[hi];
+      float tt = div_(pz, sqrt_(px * px + py * py));
+      co.eta[t] = asinh_(tt);
+    }
+  });
   std::vector<uint> flags(nT, 0u);
   std::vector<uint> counts((size_t)nT + 1, 0u);
   float dEtaCut = c.in->d_eta_cut;
-  for (uint t = 0; t < nT; ++t) {  // tripletConnectivityTightCount (:83-160)
+  const bool indexed = c.in->links_mode == 1;
+  std::unique_ptr<FollowerIndex> index(indexed ? new FollowerIndex(fo) : nullptr);
+  // a follower's flag is set by every basis that finds it: the same value,
+  // stored with relaxed atomics when bases run on several threads
+  auto set_flag = [&](uint i) { __atomic_store_n(&flags[i], 1u, __ATOMIC_RELAXED); };
+  parallel_for(nT, c.workers, 1024, [&](uint64_t b, uint64_t e, uint) {
+   for (uint t = (uint)b; t < (uint)e; ++t) {  // tripletConnectivityTightCount (:83-160)
     uint begin, end;
     if (!conn_range(c, fo, t, begin, end)) continue;
     uint inner = fo.h2[t], outer = fo.h3[t];
     float localEta = co.eta[t];
     uint cnt = 0;
-    for (uint i = begin; i < end; i++) {
-      bool test = (inner == fo.h1[i]) && (outer == fo.h2[i]) && (fabs_(localEta - co.eta[i]) < dEtaCut);
-      cnt += test;
-      if (test) flags[i] = 1;
+    if (indexed) {
+      index->each(inner, outer, begin, end, [&](uint i) {
+        if (fabs_(localEta - co.eta[i]) < dEtaCut) {
+          cnt++;
+          set_flag(i);
+        }
+      });
+    } else {
+      for (uint i = begin; i < end; i++) {
+        bool test = (inner == fo.h1[i]) && (outer == fo.h2[i]) && (fabs_(localEta - co.eta[i]) < dEtaCut);
+        cnt += test;
+        if (test) set_flag(i);
+      }
     }
     counts[t] = cnt;
-    if (cnt) flags[t] = 1;
-  }
+    if (cnt) set_flag(t);
+   }
+  });
   exclusive_scan(counts, counts.size());
   uint nLinks = counts[nT];
   if (!nLinks) {
@@ -638,7 +746,8 @@ void connectivity(const Ctx& c, const FilterOut& fo, ConnOut& co) {
   co.basis.assign(nLinks, 0u);
   co.follower.assign(nLinks, 0u);
   co.linkEvent.assign(nLinks, 0u);
-  for (uint t = 0; t < nT; ++t) {  // tripletConnectivityTightStore (:169-236)
+  parallel_for(nT, c.workers, 1024, [&](uint64_t b, uint64_t e, uint) {
+   for (uint t = (uint)b; t < (uint)e; ++t) {  // tripletConnectivityTightStore (:169-236)
     uint begin, end;
     if (!conn_range(c, fo, t, begin, end)) continue;
     uint inner = fo.h2[t], outer = fo.h3[t];
@@ -646,6 +755,19 @@ void connectivity(const Ctx& c, const FilterOut& fo, ConnOut& co) {
     uint storeOffset = counts[t];
     uint next = counts[t + 1];
     uint ev = c.h.evt[inner];
+    if (indexed) {
+      // the scan's writes for non-matching i land on the slot the next match
+      // overwrites: only the matches remain, in ascending i
+      index->each(inner, outer, begin, end, [&](uint i) {
+        if (storeOffset < next && fabs_(localEta - co.eta[i]) < dEtaCut) {
+          co.basis[storeOffset] = t;
+          co.follower[storeOffset] = i;
+          co.linkEvent[storeOffset] = ev;
+          storeOffset++;
+        }
+      });
+      continue;
+    }
     for (uint i = begin; (i < end) && (storeOffset < next); i++) {
       bool test = (inner == fo.h1[i]) && (outer == fo.h2[i]) && (fabs_(localEta - co.eta[i]) < dEtaCut);
       co.basis[storeOffset] = t;
@@ -653,7 +775,8 @@ void connectivity(const Ctx& c, const FilterOut& fo, ConnOut& co) {
       co.linkEvent[storeOffset] = ev;
       storeOffset += test;
     }
-  }
+   }
+  });
   // connectable / non-connectable index lists over the first nT-1 triplets (Q9)
   uint m = nT - 1;
   std::vector<uint> ps(flags), inv(nT, 0u);
@@ -675,7 +798,9 @@ void connectivity(const Ctx& c, const FilterOut& fo, ConnOut& co) {
 void circle_fit(const Ctx& c, const FilterOut& fo, const ConnOut& co, std::vector<float>& pt) {
   uint nT = (uint)fo.h1.size();
   pt.assign(nT, 0.0f);
-  for (uint tripletIndex : co.connectable) {
+  parallel_for(co.connectable.size(), c.workers, 4096, [&](uint64_t b, uint64_t e, uint) {
+   for (uint64_t k = b; k < e; ++k) {
+    uint tripletIndex = co.connectable[k];
     uint i0 = fo.h1[tripletIndex], i1 = fo.h2[tripletIndex], i2 = fo.h3[tripletIndex];
     trax::f3 pP0 = trax::make_f3(c.h.x[i0], c.h.y[i0], c.h.x[i0] * c.h.x[i0] + c.h.y[i0] * c.h.y[i0]);
     trax::f3 pP1 = trax::make_f3(c.h.x[i1], c.h.y[i1], c.h.x[i1] * c.h.x[i1] + c.h.y[i1] * c.h.y[i1]);
@@ -687,7 +812,8 @@ void circle_fit(const Ctx& c, const FilterOut& fo, const ConnOut& co, std::vecto
     float cc = -trax::dot3(un, pP0);
     float nz2 = un.z * un.z;
     pt[tripletIndex] = sqrt_(div_(1 - nz2 - 4 * cc * un.z, 4 * nz2));
-  }
+   }
+  });
 }
 
 // -------------------------------------------------------------------- CA
@@ -783,9 +909,10 @@ enum Stat {
   ST_PRED_TESTS_LO, ST_PRED_TESTS_HI, ST_NO_LINKS, ST_CA_CAPPED, ST_N
 };
 
-std::string run_group(const oracle_input* in, uint e0, uint e1, Group& G) {
+std::string run_group(const oracle_input* in, uint e0, uint e1, Group& G, uint workers) {
   Ctx c;
   c.in = in;
+  c.workers = workers;
   c.E = e1 - e0;
   c.L = in->n_layers;
   c.nZ = in->n_z;
@@ -838,11 +965,11 @@ std::string run_group(const oracle_input* in, uint e0, uint e1, Group& G) {
   FilterOut fo;
   filter(c, po, pr, fo);
   ConnOut co;
-  connectivity(c, fo, co);
+  if (in->links_mode != 2) connectivity(c, fo, co);
   std::vector<float> pt;
   CAOut ca;
   uint nT = (uint)fo.h1.size();
-  if (!co.noLinks) {
+  if (in->links_mode != 2 && !co.noLinks) {
     circle_fit(c, fo, co, pt);
     cellular_automaton(nT, co, pt, ca);
   }
@@ -1008,8 +1135,10 @@ int oracle_run(const oracle_input* in, oracle_result** out) {
   std::vector<std::string> errs(nGroups);
   uint nw = std::max(1u, std::min(in->n_workers, nGroups));
   if (nw <= 1) {
+    // one group at a time: the host threads work inside each group
     for (uint g = 0; g < nGroups; ++g)
-      errs[g] = run_group(in, g * G, std::min((g + 1) * G, in->n_events), r->groups[g]);
+      errs[g] = run_group(in, g * G, std::min((g + 1) * G, in->n_events), r->groups[g],
+                          std::max(1u, in->n_workers));
   } else {
     std::vector<std::thread> th;
     std::atomic<uint> next(0);
@@ -1018,7 +1147,7 @@ int oracle_run(const oracle_input* in, oracle_result** out) {
         for (;;) {
           uint g = next.fetch_add(1);
           if (g >= nGroups) break;
-          errs[g] = run_group(in, g * G, std::min((g + 1) * G, in->n_events), r->groups[g]);
+          errs[g] = run_group(in, g * G, std::min((g + 1) * G, in->n_events), r->groups[g], 1u);
         }
       });
     for (auto& t : th) t.join();

@@ -51,7 +51,13 @@ typedef struct oracle_input {
   // execution
   uint32_t n_threads;       // work-items per (event, layer pair) in pair generation; 0 = one per outer hit
   uint32_t event_grouping;  // events per group; 0 = all events in one group
-  uint32_t n_workers;       // host threads used over event groups (0 or 1 = serial)
+  uint32_t n_workers;       // host threads used over event groups (0 or 1 = serial); with one
+                            // group at a time, the threads work inside each group
+  // connectivity: 0 the reference's linear scan of the follower segment;
+  // 1 the same result through an index of the triplets by (first, second)
+  // hit (for events of hundreds of thousands of triplets); 2 no linking
+  // (connectivity, circle fit and CA skipped)
+  uint32_t links_mode;
 } oracle_input;
 
 typedef struct oracle_result oracle_result;
