@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-parity", action="store_true")
     p.add_argument("--no-align", action="store_true", help="skip the alignment (differentiable fit) measurement")
+    p.add_argument("--no-config3", action="store_true", help="skip the high-occupancy (config 3) measurement")
+    p.add_argument("--config3-steps", type=int, default=10)
     p.add_argument("--runtime-csv", default=None, help="write the timed steps as the reference's runtime csv")
     p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: autotuned)")
     p.add_argument("--no-tune", action="store_true", help="skip the autotuner (grid of the workload, default blocks)")
@@ -401,6 +403,43 @@ def run_alignment(device: int):
         ctx.close()
 
 
+def run_config3(device: int, steps: int):
+    """The high-occupancy workload at full size (16 events x 20 vertices x 1000
+    tracks, about 125 000 hits per event, grid 80 x 256): one CUDA-graph replay
+    of the whole chain per step, device time from CUDA events."""
+    from trax_gb300 import capi, events
+    batch = events.generate(3)
+    ctx = capi.Context(device)
+    try:
+        ctx.upload(batch)
+        first = ctx.seed_batch(use_graph=True)  # calibrates the capacities and captures the graph
+        for _ in range(2):
+            ctx.seed_batch(use_graph=True)
+        ms, captures = [], 0
+        for _ in range(max(steps, 1)):
+            st = ctx.seed_batch(use_graph=True)
+            ms.append(st.device_ms)
+            captures += st.graph_captures
+        t = float(np.mean(ms))
+        return {"workload": "pileup: 16 events x 20 vertices x 1000 tracks + 5% noise, 10 layers, 6 layer triplets, "
+                            "grid 80x256, seed 3 (config 3)",
+                "events_per_s": round(batch.n_events / (t * 1e-3), 2), "ms_per_batch": round(t, 3),
+                "steps": len(ms), "hits": batch.n_hits,
+                "sizes": {"pairs": st.n_pairs, "candidates": st.n_candidates, "triplets": st.n_triplets,
+                          "links": st.n_links, "track_entries": st.n_track_entries,
+                          "candidate_sentinels": st.n_candidate_sentinels},
+                "triplets_per_s": round(st.n_triplets / (t * 1e-3), 1),
+                "graph_captures": {"first_call": first.graph_captures, "timed_steps": captures,
+                                   "note": "calibrate-and-capture passes: the first call sizes every buffer from a "
+                                           "host-synced run and captures the graph; replays recapture only after "
+                                           "a capacity overflow"},
+                "kernel_launches_per_step": st.kernel_launches,
+                "parity": "tests/test_gpu_parity.py::test_pileup_workload_at_full_size: every array equals the "
+                          "oracle run on the whole batch"}
+    finally:
+        ctx.close()
+
+
 def run_ours(args, ranks):
     from trax_gb300 import capi, events
     device = ranks.local
@@ -618,6 +657,8 @@ def run_ours(args, ranks):
             result["cpu_baseline"] = cpu_baseline(batch, args.cpu_sample)
         if not args.no_align:
             result["alignment"] = run_alignment(device)
+        if not args.no_config3:
+            result["config3"] = run_config3(device, args.config3_steps)
     ctx.close()
     return result
 

@@ -84,6 +84,8 @@ typedef struct trax_batch_stats {
   uint64_t n_candidate_sentinels; /* candidate slots the reference leaves unwritten */
   uint64_t kernel_launches;       /* kernels launched by the last run */
   double device_ms;               /* device time of the last run (CUDA events) */
+  uint64_t graph_captures;        /* calibrate-and-capture passes of the last trax_seed_batch: 0 replayed the
+                                     graph, 1 built it, 2 rebuilt it after a capacity overflow */
 } trax_batch_stats;
 
 /* ---------------------------------------------------------------- context

@@ -399,3 +399,30 @@ def test_capacity_overflow_recalibrates(ctx, oracle_lib):
     st = ctx.seed_batch(use_graph=True)
     assert st.n_pairs > 2 * calibrated.n_pairs  # beyond the calibrated headroom
     compare(ctx.results(), ref)
+
+
+def test_pileup_workload_at_full_size(ctx, oracle_lib):
+    """The high-occupancy workload at full size (16 events x 20 vertices x 1000
+    tracks, about 125 000 hits per event, grid 80 x 256; 176 M pairs, 735 M
+    candidates) in one CUDA-graph replay: every array equals the oracle run on
+    the whole batch as one group (its connectivity through an index of the
+    triplets -- the same result as the reference's scan, which is quadratic
+    in segments of 290 000 triplets), on all host cores; the triplet offsets
+    are monotone and every segment's triplets sorted by (h2, h1)."""
+    import os
+    from oracle import batch_slices
+    batch = events.generate(3)
+    ctx.upload(batch)
+    st = ctx.seed_batch(use_graph=True)
+    assert st.graph_captures == 1 and st.n_candidates > 5e8
+    got = ctx.results()
+    whole = oracle_lib.run(batch, n_workers=os.cpu_count() or 1, links="indexed")[0]
+    assert batch_slices.compare_whole(got, whole) == []
+    assert np.array_equal(got["grid"], whole["grid"]) and np.array_equal(got["perm"], whole["perm"])
+    to = np.asarray(got["trip_offsets"])
+    assert np.all(np.diff(to.astype(np.int64)) >= 0)
+    h1, h2 = (np.asarray(got[k]).astype(np.uint64) for k in ("trip_h1", "trip_h2"))
+    key = (h2 << np.uint64(32)) | h1
+    seg = np.searchsorted(to, np.arange(key.size), side="right")
+    same = seg[1:] == seg[:-1]
+    assert np.all(key[1:][same] >= key[:-1][same])

@@ -67,7 +67,7 @@ class BatchStatsC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in (
         "n_hits", "n_pairs", "n_candidates", "n_triplets", "n_links", "n_connectable", "n_non_connectable",
         "n_track_entries", "n_pair_sentinels", "n_candidate_sentinels", "kernel_launches")] + [
-        ("device_ms", ctypes.c_double)]
+        ("device_ms", ctypes.c_double), ("graph_captures", ctypes.c_uint64)]
 
 
 class FitOptsC(ctypes.Structure):
@@ -200,6 +200,7 @@ class BatchStats:
     n_candidate_sentinels: int
     kernel_launches: int
     device_ms: float
+    graph_captures: int = 0
 
 
 class Context:

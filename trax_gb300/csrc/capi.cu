@@ -155,6 +155,7 @@ struct trax_ctx {
   uint64_t bufGeneration = 0;
   trax::WaitCtl wait;  // bounded-wait settings of every scan (trax_set_wait_limit, trax_debug_skip_publish)
   uint32_t graphLaunches = 0;
+  uint64_t graphCaptures = 0;  // calibrate-and-capture passes of the last trax_seed_batch
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   double lastMs = 0.0;
   // per-stage and per-kernel timing events of the last run
@@ -842,6 +843,7 @@ void fill_stats(trax_ctx* c, trax_batch_stats* s) {
   s->n_candidate_sentinels = c->candSent;
   s->kernel_launches = c->launches;
   s->device_ms = c->lastMs;
+  s->graph_captures = c->graphCaptures;
 }
 
 int copy_out(trax_ctx* c, void* dst, const DevBuf& src, size_t bytes) {
@@ -1405,6 +1407,7 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
   const bool useGraph = opts ? opts->use_graph != 0 : false;
   if (opts && opts->d_eta_cut > 0.0f) c->dEtaCut = opts->d_eta_cut;
   c->launches = 0;
+  c->graphCaptures = 0;
   c->identityHits = false;
   c->sortedSegments = true;
   if (!useGraph) {
@@ -1423,6 +1426,7 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
     const uint64_t key = shape_key(c, linking);
     if (!c->graphExec || key != c->graphKey) {
       // calibrate the capacities with one host-synced run, then capture
+      ++c->graphCaptures;
       drop_graph(c);
       RC(run_synced_chain(c, linking));
       RC(size_device_buffers(c));

@@ -76,6 +76,14 @@ __device__ __constant__ float kAsinB[12] = {3.333333333e-01f, 3.000000000e-01f, 
                                             2.237215909e-01f, 2.082331731e-01f, 1.955078125e-01f, 1.848288143e-01f,
                                             1.757089715e-01f, 1.678067162e-01f, 1.608755692e-01f, 1.547330475e-01f};
 
+// a + b = s + err exactly (Knuth's two-sum; no fused operations)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& err) {
+  const float t = a + b;
+  const float bb = t - a;
+  err = (a - (t - bb)) + (b - bb);
+  s = t;
+}
+
 // arc length s = 2R asin(r / 2R) as r + c (c returned; small next to r) and
 // ds/dR = 2 asin(x) - 2x / sqrt(1 - x^2), x = r / 2R
 __device__ __forceinline__ void arc_length(float r, float R, float& c, float& dsdR, float& sq) {
@@ -105,15 +113,28 @@ __device__ __forceinline__ bool fit_forward(const FitConfig& c, uint32_t lt, con
   f.X1 = h[0].x + k[0].dX;
   f.Y1 = h[0].y + k[0].dY;
   f.u[0] = f.v[0] = 0.0f;
+  // the chords P_i - P_1 as unevaluated sums hi + lo: the raw difference
+  // exactly (two_sum), the alignment correction added to the low part
+  float ul[3], vl[3];
+  ul[0] = vl[0] = 0.0f;
   for (int i = 1; i < 3; ++i) {
-    f.u[i] = (h[i].x - h[0].x) + (k[i].dX - k[0].dX);
-    f.v[i] = (h[i].y - h[0].y) + (k[i].dY - k[0].dY);
+    two_sum(h[i].x, -h[0].x, f.u[i], ul[i]);
+    two_sum(f.u[i], ul[i] + (k[i].dX - k[0].dX), f.u[i], ul[i]);
+    two_sum(h[i].y, -h[0].y, f.v[i], vl[i]);
+    two_sum(f.v[i], vl[i] + (k[i].dY - k[0].dY), f.v[i], vl[i]);
   }
   for (int i = 0; i < 3; ++i) f.Z[i] = h[i].z + c.dz[c.layer[i][lt]];
   const float u2 = f.u[1], v2 = f.v[1], u3 = f.u[2], v3 = f.v[2];
   f.q2 = u2 * u2 + v2 * v2;
   f.q3 = u3 * u3 + v3 * v3;
-  f.D = 2.0f * (u2 * v3 - u3 * v2);
+  // D = 2 (u2 v3 - u3 v2): for a nearly straight triplet the two products
+  // almost cancel (by about the chord length over 2R), so D takes the exact
+  // errors of both products (FMA) and the chords' low parts; the curvature
+  // then stays within about 1e-6 of FP64
+  const float p23 = u2 * v3, p32 = u3 * v2;
+  const float e23 = __fmaf_rn(u2, v3, -p23), e32 = __fmaf_rn(u3, v2, -p32);
+  const float corr = (e23 - e32) + ((u2 * vl[2] + ul[1] * v3) - (u3 * vl[1] + ul[2] * v2));
+  f.D = 2.0f * ((p23 - p32) + corr);
   f.a = (v3 * f.q2 - v2 * f.q3) / f.D;
   f.b = (u2 * f.q3 - u3 * f.q2) / f.D;
   f.R = sqrtf(f.a * f.a + f.b * f.b);
