@@ -49,23 +49,44 @@ def test_fit_rows_are_truth_matched_and_grouped(small):
     assert np.all(np.diff(lt.astype(np.int64)) >= 0)  # rows ordered by layer triplet
 
 
-def test_fit_params_and_chi2_match_fp64(small, align_ref):
+# Each fit parameter's error against FP64 (on the same FP32 hits), relative
+# to its natural scale: the curvature to |kappa| + 1e-4 / cm (a 114 GeV track
+# in 3.8 T, below the triplets' curvature resolution: kappa -> 0 is a
+# straight track, where a bare relative error has no meaning); cot(theta) to
+# max(|t|, 1); the impact parameter d0 to |d0| + r1, the lever arm from the
+# first hit to the beam line; z0 to |z0| + r1 max(|t|, 1), the length of the
+# extrapolation from the first hit.  The bar is 1e-5 for each, worst row.
+KAPPA_FLOOR = 1e-4
+
+
+def fit_param_errors(params, p64, r1):
+    P = params.astype(np.float64)
+    k, d0, z0, t = (p64[:, i] for i in range(4))
+    return {"kappa": np.abs(P[:, 0] - k) / (np.abs(k) + KAPPA_FLOOR),
+            "d0": np.abs(P[:, 1] - d0) / (np.abs(d0) + r1),
+            "z0": np.abs(P[:, 2] - z0) / (np.abs(z0) + r1 * np.maximum(np.abs(t), 1.0)),
+            "cot_theta": np.abs(P[:, 3] - t) / np.maximum(np.abs(t), 1.0),
+            "kappa_relative": np.abs(P[:, 0] - k) / np.abs(k)}
+
+
+@pytest.mark.parametrize("at", ["zero", "shifted"])
+def test_fit_params_and_chi2_match_fp64(small, align_ref, at):
     batch, ctx, ref, _ = small
     a = np.zeros((batch.n_layers, 3))
+    if at == "shifted":
+        rng = np.random.default_rng(3)
+        a = np.stack([rng.normal(0, 0.003, batch.n_layers), rng.normal(0, 0.003, batch.n_layers),
+                      rng.normal(0, 1e-5, batch.n_layers)], axis=1)
     chi2, params = ctx.fit_forward(a, params=True)
     p64 = align_ref.triplet_params(ref["x"], ref["y"], ref["z"], ref["layer"], ref["h1"], ref["h2"], ref["h3"], a)
     l64 = align_ref.loss(*_ref_args(ref), a, ref["sigma_tip"], 0.002)
     assert abs(chi2 - l64) <= 1e-4 * l64
-    rel_k = np.abs(params[:, 0] - p64[:, 0]) / np.abs(p64[:, 0])
-    rel_t = np.abs(params[:, 3] - p64[:, 3]) / np.maximum(np.abs(p64[:, 3]), 1e-3)
-    d_d0 = np.abs(params[:, 1] - p64[:, 1])
-    d_z0 = np.abs(params[:, 2] - p64[:, 2])
-    # FP32 against FP64 on the same FP32 hits: curvature and cot(theta) to a
-    # few 1e-6 relative at the median, d0 and z0 to well below a micron
-    assert np.median(rel_k) < 1e-5 and np.quantile(rel_k, 0.99) < 1e-3
-    assert np.median(rel_t) < 1e-5 and np.quantile(rel_t, 0.99) < 1e-4
-    assert np.median(d_d0) < 1e-5 and np.quantile(d_d0, 0.99) < 1e-4
-    assert np.median(d_z0) < 1e-5 and np.quantile(d_z0, 0.99) < 1e-4
+    r1 = np.hypot(ref["x"][ref["h1"]], ref["y"][ref["h1"]])
+    err = fit_param_errors(params, p64, r1)
+    # measured worst rows: 8.4e-7 (kappa), 3.3e-7 (d0), 6.5e-7 (z0), 4.7e-7 (cot theta)
+    for k in ("kappa", "d0", "z0", "cot_theta"):
+        assert err[k].max() <= 1e-5, (k, float(err[k].max()))
+    assert np.median(err["kappa_relative"]) <= 1e-6
 
 
 @pytest.mark.parametrize("at", ["zero", "shifted"])
@@ -96,7 +117,8 @@ def test_hit_gradient_matches_fp64_adjoint(small, align_ref):
     want = np.zeros_like(gh64)
     want[perm] = gh64  # grid order -> input order
     assert gh.shape == want.shape
-    assert np.linalg.norm(gh - want) <= 1e-3 * np.linalg.norm(want)
+    # measured 1.6e-4 (the FP32 reverse pass through the circle and arc lengths)
+    assert np.linalg.norm(gh - want) <= 3e-4 * np.linalg.norm(want)
     # hits that are in no fit row have zero gradient
     used = np.zeros(batch.n_hits, bool)
     used[perm[np.concatenate([ref["h1"], ref["h2"], ref["h3"]])]] = True
