@@ -196,14 +196,19 @@ def peaks():
 
 # Algorithmic bytes of the timed kernels: compulsory streams only (each input
 # array read once, each output written once), from the sizes of the run.  The
-# packed (x, y, z, phi) hit array is 16 B per hit, the grid 4 B per cell.
-def kernel_bytes(name, st, n_tasks, n_hits, cells):
+# packed (x, y, z, phi) hit array is 16 B per hit, the grid 4 B per cell; the
+# pair kernels read the cells of the inner layers only, the prediction those
+# of the third layers (cells_inner, cells_third: the layers' cells of all
+# events).
+def kernel_bytes(name, st, n_tasks, n_hits, cells, cells_inner=None, cells_third=None):
     P, Cc, T = st.n_pairs, st.n_candidates, st.n_triplets
+    ci = cells if cells_inner is None else cells_inner
+    c3 = cells if cells_third is None else cells_third
     return {
         "grid_build": 56 * n_hits + 4 * cells,
-        "pair_count": 16 * n_hits + 4 * cells + 4 * n_tasks,
-        "pair_store": 16 * n_hits + 4 * cells + 4 * n_tasks + 8 * P,
-        "predict_count": 16 * n_hits + 4 * cells + 8 * P + 4 * P,
+        "pair_count": 16 * n_hits + 4 * ci + 4 * n_tasks,
+        "pair_store": 16 * n_hits + 4 * ci + 4 * n_tasks + 8 * P,
+        "predict_count": 16 * n_hits + 4 * c3 + 8 * P + 4 * P,
         "predict_store": 8 * P + 4 * P + 8 * Cc,
         "filter": 16 * n_hits + 8 * P + 8 * Cc + 4 * Cc,
         "filter_store": 8 * P + 8 * Cc + 4 * Cc + 12 * T,
@@ -507,7 +512,10 @@ def run_ours(args, ranks):
     # pair-stage tasks: one per outer-layer hit of every (event, layer triplet)
     n_tasks = int(sum(int(batch.layer_hits[:, lt.layer2 - 1].sum()) for lt in batch.lts))
     hbm, peak_kind = peaks()
-    kb = kernel_bytes(dom, st, n_tasks, n_hits, cells)
+    per_layer = batch.n_events * (batch.n_z + 1) * (batch.n_phi + 1)
+    cells_inner = per_layer * len({lt.layer1 for lt in batch.lts})
+    cells_third = per_layer * len({lt.layer3 for lt in batch.lts})
+    kb = kernel_bytes(dom, st, n_tasks, n_hits, cells, cells_inner, cells_third)
     achieved = kb / (kmean[dom] * 1e-3) / 1e9
     cb = chain_bytes(st, n_hits, cells, len(batch.lts))
     result = {
@@ -518,6 +526,7 @@ def run_ours(args, ranks):
                                "triplets, seed 2 (config 2)",
                    "events_per_gpu": batch.n_events, "hits_per_gpu": n_hits, "grid": f"{batch.n_z}x{batch.n_phi}",
                    "block_sizes": {k: shape[k] for k in ("pair_threads", "predict_threads", "filter_threads")},
+                   "predict_pairs_per_thread": ctx.pairs_per_thread(),
                    "autotune": None if tune is None else {
                        "shapes_timed": tune["shapes_timed"], "from_cache": bool(tune["from_cache"]),
                        "best_ms": round(tune["best_ms"], 4), "default_shape_ms": round(tune["default_ms"], 4)},
@@ -596,6 +605,7 @@ def run_ours(args, ranks):
             c2.set_grid(shape_now["n_z"], shape_now["n_phi"])
             c2.set_block_sizes(shape_now["pair_threads"], shape_now["predict_threads"],
                                shape_now["filter_threads"])
+            c2.set_pairs_per_thread(ctx.pairs_per_thread())
             for _w in range(2):
                 c2.seed_batch(use_graph=True)
             outs = ([capi.pinned_empty((max(st.n_triplets, 1),), np.uint32) for _ in range(3)]

@@ -241,6 +241,14 @@ int trax_noalloc_set_wait(uint32_t polls, uint32_t skip_tile);
 int trax_set_block_sizes(trax_ctx* ctx, uint32_t pair_threads, uint32_t predict_threads, uint32_t filter_threads);
 /* out5 = n_z, n_phi, pair threads, prediction threads, filter threads. */
 int trax_get_launch_config(trax_ctx* ctx, uint32_t* out5);
+/* Pairs per thread of the prediction's count pass: 1, 2 or 4 (default 1).
+ * With k > 1 a thread computes the windows of k pairs and walks their
+ * candidate hits in one loop, which evens out the work of a warp's threads;
+ * the results do not change.  No counterpart in the reference, where one
+ * work-item takes one pair (TripletThetaPhiPredictor.cpp:22-41); trax_autotune
+ * tunes it after the block sizes. */
+int trax_set_pairs_per_thread(trax_ctx* ctx, uint32_t k);
+int trax_get_pairs_per_thread(trax_ctx* ctx, uint32_t* k);
 
 /* ------------------------------------------------------------- batched
  * The whole chain (buildTriplets, TripletBuilder.cpp:312-467) for all
@@ -270,6 +278,7 @@ typedef struct trax_tune_result {
   uint32_t pair_threads, predict_threads, filter_threads;
   uint32_t from_cache;       /* 1: taken from the cache file */
   uint32_t shapes_timed;     /* shapes timed by this call */
+  uint32_t pairs_per_thread; /* of the prediction count (trax_set_pairs_per_thread) */
   double best_ms;            /* device time of one chain replay at the chosen shape */
   double default_ms;         /* the same for the shape the context had before */
 } trax_tune_result;

@@ -45,6 +45,26 @@ def test_grid_sizes_around_shared_memory_limit(ctx, oracle_lib, grid):
     compare(ctx.results(), ref)
 
 
+@pytest.mark.parametrize("k", [2, 4])
+def test_pairs_per_thread_keep_results(ctx, oracle_lib, k):
+    """The prediction count with K pairs per thread (windows staged in shared
+    memory, one flat walk per lane) writes the same counts, offsets and kept
+    candidates as one pair per thread, at several block sizes."""
+    batch = events.generate(2, n_events=12)
+    ref = oracle_lib.run(batch)[0]
+    ctx.upload(batch)
+    try:
+        for blocks in [(256, 64, 256), (128, 128, 128), (128, 256, 128)]:
+            ctx.set_block_sizes(*blocks)
+            ctx.set_pairs_per_thread(k)
+            assert ctx.pairs_per_thread() == k
+            ctx.seed_batch(use_graph=True)
+            compare(ctx.results(), ref)
+    finally:
+        ctx.set_pairs_per_thread(1)
+        ctx.set_block_sizes(128, 128, 256)
+
+
 def test_invalid_block_sizes_rejected(ctx, trax_lib):
     for bad in [(0, 128, 128), (33, 128, 128), (128, 512, 128), (128, 128, 16)]:
         with pytest.raises(trax_lib.TraxError) as e:
@@ -69,8 +89,10 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
         ref = oracle_lib.run(batch)[0]
         c.seed_batch(use_graph=True)
         compare(c.results(), ref)
+        assert res["pairs_per_thread"] in (1, 2, 4) and c.pairs_per_thread() == res["pairs_per_thread"]
         entries = json.loads(cache.read_text())["entries"]
         assert len(entries) == 1 and entries[0]["n_z"] == res["n_z"] and entries[0]["sm_count"] > 0
+        assert entries[0]["pairs_per_thread"] == res["pairs_per_thread"]
     finally:
         c.close()
     # a new context with the same workload takes the cached shape without timing
@@ -79,12 +101,31 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
         c.upload(events.generate(1, n_events=20))
         res2 = c.autotune(cache_path=str(cache), search_grid=True, replays=1)
         assert res2["from_cache"] == 1 and res2["shapes_timed"] == 0
-        assert [res2[k] for k in ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads")] == \
-               [res[k] for k in ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads")]
+        keys = ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "pairs_per_thread")
+        assert [res2[k] for k in keys] == [res[k] for k in keys]
         # a different workload gets its own entry
         c.upload(events.generate(1, n_events=21))
         res3 = c.autotune(cache_path=str(cache), search_grid=False, replays=1)
         assert res3["from_cache"] == 0
         assert len(json.loads(cache.read_text())["entries"]) == 2
+    finally:
+        c.close()
+
+
+def test_autotune_cache_entry_without_pairs_per_thread(trax_lib, tmp_path):
+    """Cache files written before the pairs-per-thread axis existed still load (as 1)."""
+    batch = events.generate(1, n_events=20)
+    cache = tmp_path / "tune.json"
+    c = trax_lib.Context(0)
+    try:
+        c.upload(batch)
+        c.autotune(cache_path=str(cache), search_grid=False, replays=1)
+        doc = json.loads(cache.read_text())
+        for e in doc["entries"]:
+            e.pop("pairs_per_thread")
+        cache.write_text(json.dumps(doc))
+        c.set_pairs_per_thread(4)
+        res = c.autotune(cache_path=str(cache), search_grid=False, replays=1)
+        assert res["from_cache"] == 1 and res["pairs_per_thread"] == 1 and c.pairs_per_thread() == 1
     finally:
         c.close()

@@ -35,7 +35,8 @@ EXPORTED = [
     "trax_events_upload", "trax_physics_triplets_device", "trax_physics_tracks_device",
     "trax_physics_triplets", "trax_physics_tracks", "trax_geometry_from_files", "trax_host_alloc",
     "trax_host_free", "trax_set_wait_limit", "trax_debug_skip_publish", "trax_noalloc_set_wait",
-    "trax_circle_fit_on", "trax_get_pt", "trax_cellular_automaton_on",
+    "trax_circle_fit_on", "trax_get_pt", "trax_cellular_automaton_on", "trax_set_pairs_per_thread",
+    "trax_get_pairs_per_thread",
 ]
 
 
@@ -80,7 +81,8 @@ class TuneOptsC(ctypes.Structure):
 
 class TuneResultC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint32) for n in (
-        "n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "from_cache", "shapes_timed")] + [
+        "n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "from_cache", "shapes_timed",
+        "pairs_per_thread")] + [
         ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
 
 
@@ -122,6 +124,8 @@ def load() -> ctypes.CDLL:
             "trax_circle_fit": ([vp], i32),
             "trax_cellular_automaton": ([vp, pu64], i32),
             "trax_prefix_sum": ([vp, vp, u64], i32),
+            "trax_set_pairs_per_thread": ([vp, u32], i32),
+            "trax_get_pairs_per_thread": ([vp, vp], i32),
             "trax_set_wait_limit": ([vp, u32], i32),
             "trax_circle_fit_on": ([vp, vp, u64], i32),
             "trax_get_pt": ([vp, vp], i32),
@@ -340,6 +344,15 @@ class Context:
 
     def set_block_sizes(self, pair_threads: int, predict_threads: int, filter_threads: int):
         self._check(self._L.trax_set_block_sizes(self._h, pair_threads, predict_threads, filter_threads))
+
+    def set_pairs_per_thread(self, k: int):
+        """Pairs per thread of the prediction's count pass (1, 2 or 4)."""
+        self._check(self._L.trax_set_pairs_per_thread(self._h, k))
+
+    def pairs_per_thread(self) -> int:
+        k = ctypes.c_uint32()
+        self._check(self._L.trax_get_pairs_per_thread(self._h, ctypes.byref(k)))
+        return int(k.value)
 
     def launch_config(self) -> Dict[str, int]:
         """Current grid and block sizes: n_z, n_phi, pair/predict/filter threads."""

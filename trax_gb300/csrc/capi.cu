@@ -107,6 +107,7 @@ struct trax_ctx {
   std::vector<float> minR, maxR;
   uint32_t nZ = 0, nP = 0;
   uint32_t pairThreads = 128, predThreads = 128, filterThreads = 256;  // launch shape
+  uint32_t predK = 1;  // pairs per thread of the prediction count pass
   bool haveLT = false, haveGeom = false, haveGrid = false, haveHits = false;
   bool cfgDirty = true;  // layer triplets or geometry changed since the device configuration was built
   // batch shape
@@ -126,7 +127,7 @@ struct trax_ctx {
   // grid stage
   DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
   // pair stage
-  DevBuf segOuter, taskBase, taskCount, taskOrdered, pairs, pairOffsets;
+  DevBuf segOuter, taskBase, taskCount, taskState, pairs, pairOffsets;
   // prediction / filter
   DevBuf candLocal, predWarps, predKeep, cands, candOffsets, flagWords, flagSums, h1, h2, h3, tripOffsets;
   // connectivity / fit / CA
@@ -302,6 +303,7 @@ int build_config(trax_ctx* c, bool seeding = true) {
   g.pairThreads = c->pairThreads;
   g.predThreads = c->predThreads;
   g.filterThreads = c->filterThreads;
+  g.predPairsPerThread = c->predK;
   for (uint32_t p = 0; p < g.nLT; ++p) {
     const trax_layer_triplet& t = c->lts[p];
     if (t.layer1 < 1 || t.layer2 < 1 || t.layer3 < 1 || t.layer1 > c->L || t.layer2 > c->L || t.layer3 > c->L)
@@ -438,12 +440,12 @@ int stage_pairs(trax_ctx* c, Mode mode) {
     maxTasks = c->nTasks;
   }
   ENSURE(taskCount, maxTasks + 1, 4);
-  ENSURE(taskOrdered, maxTasks + 1, 1);
+  ENSURE(taskState, pair_task_state_bytes(maxTasks) + 16, 1);
   uint32_t* taskCount = ptr<uint32_t>(c->taskCount);
-  uint8_t* taskOrdered = ptr<uint8_t>(c->taskOrdered);
+  const PairTaskState taskState = pair_task_state(c->taskState.p, maxTasks);
   KBEG(TK_PAIR_COUNT);
   CK(pair_tasks(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
-                maxTasks, taskCount, taskOrdered, nullptr, 0, slot(c, S_PAIR_SENT), dev_err(c), c->st,
+                maxTasks, taskCount, taskState, nullptr, 0, slot(c, S_PAIR_SENT), dev_err(c), c->st,
                 &c->launches));
   KEND(TK_PAIR_COUNT);
   RC(scan_publish(c, mode, taskCount, c->nTasks, mode == DEVICE ? nTasksDev : nullptr, maxTasks, S_PAIRS,
@@ -456,7 +458,7 @@ int stage_pairs(trax_ctx* c, Mode mode) {
   ENSURE(pairs, maxPairs, 8);
   KBEG(TK_PAIR_EMIT);
   CK(pair_tasks(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint32_t>(c->segOuter), taskBase, nTasksDev,
-                maxTasks, taskCount, taskOrdered, ptr<uint2>(c->pairs), maxPairs, slot(c, S_PAIR_SENT), dev_err(c),
+                maxTasks, taskCount, taskState, ptr<uint2>(c->pairs), maxPairs, slot(c, S_PAIR_SENT), dev_err(c),
                 c->st, &c->launches));
   KEND(TK_PAIR_EMIT);
   CK(pair_offsets(c->cfg, taskBase, taskCount, ptr<uint32_t>(c->pairOffsets), c->st, &c->launches));
@@ -741,7 +743,7 @@ int size_device_buffers(trax_ctx* c) {
   c->capTracks = with_headroom(c->nTracks);
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   ENSURE(taskCount, c->capTasks + 1, 4);
-  ENSURE(taskOrdered, c->capTasks + 1, 1);
+  ENSURE(taskState, pair_task_state_bytes(c->capTasks) + 16, 1);
   ENSURE(pairs, c->capPairs, 8);
   ENSURE(candLocal, c->capPairs + 1, 4);
   ENSURE(predWarps, (c->capPairs + 31) / 32 + 1, 4);
@@ -950,7 +952,7 @@ void trax_destroy(trax_ctx* c) {
                     &c->trk_compStart, &c->trk_cursor, &c->trk_members, &c->trk_filtered, &c->trk_hits,
                     &c->trk_entryTrack, &c->trk_owner, &c->trk_table, &c->trk_counts, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
-                    &c->segOuter, &c->taskBase, &c->taskCount, &c->taskOrdered, &c->pairs, &c->pairOffsets, &c->candLocal, &c->predWarps, &c->predKeep, &c->cands,
+                    &c->segOuter, &c->taskBase, &c->taskCount, &c->taskState, &c->pairs, &c->pairOffsets, &c->candLocal, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->linkRun, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS, &c->connW, &c->nonConnW,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,
@@ -1028,6 +1030,19 @@ int trax_set_block_sizes(trax_ctx* c, uint32_t pair_threads, uint32_t predict_th
   c->pairThreads = pair_threads;
   c->predThreads = predict_threads;
   c->filterThreads = filter_threads;
+  return TRAX_OK;
+}
+
+int trax_set_pairs_per_thread(trax_ctx* c, uint32_t k) {
+  if (!c) return TRAX_ERR_ARG;
+  if (k != 1 && k != 2 && k != 4) return fail(c, TRAX_ERR_ARG, "pairs per thread must be 1, 2 or 4");
+  c->predK = k;
+  return TRAX_OK;
+}
+
+int trax_get_pairs_per_thread(trax_ctx* c, uint32_t* k) {
+  if (!c || !k) return TRAX_ERR_ARG;
+  *k = c->predK;
   return TRAX_OK;
 }
 

@@ -188,17 +188,39 @@ template <bool EMIT>
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     pair_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                 const uint32_t* __restrict__ segOuter, const uint32_t* __restrict__ taskBase,
-                const uint32_t* __restrict__ nTasksDev, uint32_t* taskCount, uint8_t* orderedRows, uint2* pairs,
+                const uint32_t* __restrict__ nTasksDev, uint32_t* taskCount, PairTaskState state, uint2* pairs,
                 uint32_t capPairs, uint32_t* sentinels, uint32_t* err) {
   const uint32_t S = cfg.E * cfg.nLT;
   const uint32_t nTasks = *nTasksDev;
   const uint32_t C = cfg.C, nP = cfg.nP;
   for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < nTasks; k += gridDim.x * blockDim.x) {
-    const uint32_t s = find_segment(taskBase, S, k);
+    uint32_t s, i;
+    PairWindow w;
+    bool ordered = false;
+    if (!EMIT) {
+      s = find_segment(taskBase, S, k);
+      i = segOuter[s] + (k - taskBase[s]);
+      const float4 ho = hits[i];
+      w = pair_window(cfg, s % cfg.nLT, ho.x, ho.y, ho.z, ho.w);
+    } else {
+      // the count pass's window, segment and ordering of this task
+      const float4 b = state.bounds[k];
+      const uint4 q = state.secs[k];
+      const uint2 id = state.ids[k];
+      i = id.x;
+      s = id.y;
+      w.zLow = b.x;
+      w.zHigh = b.y;
+      w.phiLow = b.z;
+      w.phiHigh = b.w;
+      w.zLowSector = q.x & 0x7fffffffu;
+      w.zHighSector = q.y & 0x7fffffffu;
+      w.pL = q.z;
+      w.pH = q.w;
+      w.wrap = q.y >> 31;
+      ordered = (q.x >> 31) != 0u;
+    }
     const uint32_t e = s / cfg.nLT, p = s % cfg.nLT;
-    const uint32_t i = segOuter[s] + (k - taskBase[s]);
-    const float4 ho = hits[i];
-    const PairWindow w = pair_window(cfg, p, ho.x, ho.y, ho.z, ho.w);
     const uint32_t* lG1 = grid + ((size_t)e * cfg.L + (cfg.layer1[p] - 1)) * C;
     if (!EMIT) {
       uint32_t nFound = 0;
@@ -213,7 +235,10 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
         for (uint32_t j = a2; j < b2; ++j) nFound += pair_valid(w, hits[j]);
       }
       taskCount[k] = nFound;
-      orderedRows[k] = simple ? 1 : 0;
+      state.bounds[k] = make_float4(w.zLow, w.zHigh, w.phiLow, w.phiHigh);
+      state.secs[k] = make_uint4(w.zLowSector | (simple ? 0x80000000u : 0u), w.zHighSector | (w.wrap << 31), w.pL,
+                                 w.pH);
+      state.ids[k] = make_uint2(i, s);
     } else {
       const uint32_t pos0 = taskCount[k];
       uint32_t limit = taskCount[k + 1] - pos0;
@@ -221,7 +246,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
       else if (limit > capPairs - pos0) limit = capPairs - pos0;
       uint2* out = pairs + pos0;
       // the count pass checked the ordering of the ranges
-      const bool simple = orderedRows[k] != 0;
+      const bool simple = ordered;
       uint32_t written = 0;
       if (simple) {
         // the common path tests (z, phi) pairs: 8 bytes per visited hit
@@ -295,7 +320,7 @@ cudaError_t pair_segments(const DevConfig& cfg, const uint32_t* grid, uint32_t* 
 
 cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint32_t* segOuter,
                        const uint32_t* taskBase, const uint32_t* nTasksDev, uint64_t maxTasks, uint32_t* taskCount,
-                       uint8_t* orderedRows, uint2* pairs, uint64_t capPairs, uint32_t* sentinels, uint32_t* err,
+                       PairTaskState state, uint2* pairs, uint64_t capPairs, uint32_t* sentinels, uint32_t* err,
                        cudaStream_t st, uint32_t* launches) {
   const uint32_t cap = capPairs > 0xffffffffull ? 0xffffffffu : (uint32_t)capPairs;
   if (emit && maxTasks == 0) return cudaSuccess;
@@ -303,10 +328,10 @@ cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, De
   const int blocks = grid_for(maxTasks + 1, threads);
   if (emit)
     pair_kernel<true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
-                                                       taskCount, orderedRows, pairs, cap, sentinels, err);
+                                                       taskCount, state, pairs, cap, sentinels, err);
   else
     pair_kernel<false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, segOuter, taskBase, nTasksDev,
-                                                        taskCount, orderedRows, pairs, cap, sentinels, err);
+                                                        taskCount, state, pairs, cap, sentinels, err);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

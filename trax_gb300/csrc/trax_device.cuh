@@ -37,6 +37,7 @@ struct DevConfig {
   // launch shape chosen by the autotuner (threads per block of the pair,
   // prediction and filter kernels; at most TRAX_MAX_TUNED_THREADS)
   uint32_t pairThreads, predThreads, filterThreads;
+  uint32_t predPairsPerThread;  // 1, 2 or 4 pairs per thread in the prediction count pass
 };
 
 #define TRAX_MAX_TUNED_THREADS 256

@@ -136,13 +136,31 @@ cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStre
 // Per (event, layer triplet) segment: first outer hit and number of outer hits.
 cudaError_t pair_segments(const DevConfig& cfg, const uint32_t* grid, uint32_t* segOuter, uint32_t* segCount,
                           cudaStream_t st, uint32_t* launches);
+// What the count pass leaves for the store pass per outer-hit task k, so
+// that the store pass neither searches the task's segment nor recomputes
+// its window: bounds[k] = (zLow, zHigh, phiLow, phiHigh);
+// secs[k] = (zLowSector | ordered << 31, zHighSector | wrap << 31, pL, pH),
+// `ordered` when the task's visit ranges are disjoint and ascending
+// (zLowSector <= INT32_MAX, zHighSector <= nZ < 2^22); ids[k] = (outer hit,
+// segment).  pair_task_state_bytes(n) bytes hold the arrays of n tasks.
+struct PairTaskState {
+  float4* bounds;
+  uint4* secs;
+  uint2* ids;
+};
+inline size_t pair_task_state_bytes(uint64_t n) { return (size_t)n * 40u; }
+inline PairTaskState pair_task_state(void* base, uint64_t n) {
+  char* b = static_cast<char*>(base);
+  return PairTaskState{reinterpret_cast<float4*>(b), reinterpret_cast<uint4*>(b + 16 * n),
+                       reinterpret_cast<uint2*>(b + 32 * n)};
+}
+
 // Count (emit == false) or store (emit == true) pairs of every outer-hit task.
 // taskBase[S+1] is the exclusive scan of segCount; nTasksDev = &taskBase[S].
-// orderedRows[k]: whether task k's visit ranges are disjoint and ascending
-// (written by the count pass, read by the store pass)
+// The count pass writes `state`, the store pass reads it.
 cudaError_t pair_tasks(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits,
                        const uint32_t* segOuter, const uint32_t* taskBase, const uint32_t* nTasksDev,
-                       uint64_t maxTasks, uint32_t* taskCount, uint8_t* orderedRows, uint2* pairs,
+                       uint64_t maxTasks, uint32_t* taskCount, PairTaskState state, uint2* pairs,
                        uint64_t capPairs, uint32_t* sentinelCount, uint32_t* err, cudaStream_t st,
                        uint32_t* launches);
 // pairOffsets[s+1] = first pair of segment s+1 (Pairing::pairingOffsets)

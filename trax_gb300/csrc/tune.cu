@@ -24,13 +24,20 @@ namespace {
 
 struct Shape {
   uint32_t nZ, nP, pairT, predT, filtT;
+  uint32_t predK;  // pairs per thread of the prediction count
 };
+
+int apply_shape(trax_ctx* c, const Shape& s) {
+  int rc = trax_set_grid(c, s.nZ, s.nP);
+  if (rc == TRAX_OK) rc = trax_set_block_sizes(c, s.pairT, s.predT, s.filtT);
+  if (rc == TRAX_OK) rc = trax_set_pairs_per_thread(c, s.predK);
+  return rc;
+}
 
 // Device milliseconds of one replay at `s` (best of `replays`), or a negative
 // value when the shape cannot run (its status is returned in *rc).
 double time_shape(trax_ctx* c, const Shape& s, bool linking, int replays, int* rc) {
-  *rc = trax_set_grid(c, s.nZ, s.nP);
-  if (*rc == TRAX_OK) *rc = trax_set_block_sizes(c, s.pairT, s.predT, s.filtT);
+  *rc = apply_shape(c, s);
   if (*rc != TRAX_OK) return -1.0;
   trax_batch_opts o;
   o.use_graph = 1;
@@ -116,7 +123,9 @@ bool cache_lookup(const char* path, const std::string& key, Shape* s, double* ms
     if (!field_u64(e, "n_z", &v[0]) || !field_u64(e, "n_phi", &v[1]) || !field_u64(e, "pair_threads", &v[2]) ||
         !field_u64(e, "predict_threads", &v[3]) || !field_u64(e, "filter_threads", &v[4]))
       continue;
-    *s = Shape{(uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3], (uint32_t)v[4]};
+    unsigned long long ppt = 1;  // entries written before the axis existed
+    field_u64(e, "pairs_per_thread", &ppt);
+    *s = Shape{(uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3], (uint32_t)v[4], (uint32_t)ppt};
     if (!field_f64(e, "ms", ms)) *ms = 0.0;
     return true;
   }
@@ -132,8 +141,8 @@ bool cache_store(const char* path, const std::string& key, int sms, const Shape&
   char b[512];
   snprintf(b, sizeof(b),
            "{\"key\": \"%s\", \"sm_count\": %d, \"n_z\": %u, \"n_phi\": %u, \"pair_threads\": %u, "
-           "\"predict_threads\": %u, \"filter_threads\": %u, \"ms\": %.6f}",
-           key.c_str(), sms, s.nZ, s.nP, s.pairT, s.predT, s.filtT, ms);
+           "\"predict_threads\": %u, \"filter_threads\": %u, \"pairs_per_thread\": %u, \"ms\": %.6f}",
+           key.c_str(), sms, s.nZ, s.nP, s.pairT, s.predT, s.filtT, s.predK, ms);
   keep.push_back(b);
   const std::string tmp = std::string(path) + ".tmp";
   {
@@ -166,10 +175,11 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, trax::ctx_device(c));
 
-  uint32_t cur[5];
+  uint32_t cur[5], curK = 1;
   int rc = trax_get_launch_config(c, cur);
+  if (rc == TRAX_OK) rc = trax_get_pairs_per_thread(c, &curK);
   if (rc != TRAX_OK) return rc;
-  const Shape start{cur[0], cur[1], cur[2], cur[3], cur[4]};
+  const Shape start{cur[0], cur[1], cur[2], cur[3], cur[4], curK};
 
   uint64_t h = trax::workload_hash(c);
   h ^= (uint64_t)sms * 0x9e3779b97f4a7c15ull;
@@ -182,8 +192,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
   Shape best = start;
   double bestMs = -1.0;
   if (cache_path && cache_lookup(cache_path, key, &best, &bestMs)) {
-    rc = trax_set_grid(c, best.nZ, best.nP);
-    if (rc == TRAX_OK) rc = trax_set_block_sizes(c, best.pairT, best.predT, best.filtT);
+    rc = apply_shape(c, best);
     if (rc != TRAX_OK) return rc;
     res.from_cache = 1;
     res.best_ms = bestMs;
@@ -211,7 +220,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
         for (uint32_t p : ps) {
           if ((z + 1) * (p + 1) > TRAX_GRID_SMEM_CELLS) continue;
           if (z == start.nZ && p == start.nP) continue;
-          consider(Shape{z, p, best.pairT, best.predT, best.filtT});
+          consider(Shape{z, p, best.pairT, best.predT, best.filtT, best.predK});
         }
     }
     static const uint32_t ts[] = {64, 96, 128, 192, 256};
@@ -223,8 +232,16 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
         *f = t;
         consider(s);
       }
-    rc = trax_set_grid(c, best.nZ, best.nP);
-    if (rc == TRAX_OK) rc = trax_set_block_sizes(c, best.pairT, best.predT, best.filtT);
+    // pairs per thread of the prediction count, at the chosen block size
+    static const uint32_t ks[] = {1, 2, 4};
+    const Shape byBlocks = best;
+    for (uint32_t k : ks) {
+      if (k == byBlocks.predK) continue;
+      Shape s = byBlocks;
+      s.predK = k;
+      consider(s);
+    }
+    rc = apply_shape(c, best);
     if (rc != TRAX_OK) return rc;
     res.best_ms = bestMs;
     if (cache_path && !cache_store(cache_path, key, sms, best, bestMs)) {
@@ -237,6 +254,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
   res.pair_threads = best.pairT;
   res.predict_threads = best.predT;
   res.filter_threads = best.filtT;
+  res.pairs_per_thread = best.predK;
   if (result) *result = res;
   return TRAX_OK;
 }
