@@ -234,6 +234,18 @@ int trax_set_wait_limit(trax_ctx* ctx, uint32_t polls);
 int trax_debug_skip_publish(trax_ctx* ctx, uint32_t tile);
 int trax_noalloc_set_wait(uint32_t polls, uint32_t skip_tile);
 
+/* The library's single-precision math evaluated on the device `device`:
+ * out[i] = fn(a[i], b[i]) for n elements of host arrays, synchronously.  No
+ * counterpart in the reference; the kernels evaluate OpenCL's atan2, acos,
+ * atan and the float->integer conversions (e.g. PairGeneratorBeamspot.h:111-162,
+ * TripletThetaPhiFilter.h:118-128) with these definitions, so that their
+ * results are the same on every device.  fn: 0 atan2(a, b), 1 acos, 2 atan,
+ * 3 asinh, 4 log, 5 a / b, 6 sqrt, 7 floor, 8 saturating float->uint32 and
+ * 9 float->int32 (truncation, NaN -> 0; out holds the integer's bits);
+ * 10-14 CUDA's own atan2f, acosf, atanf, asinhf, logf for comparison.
+ * b may be null unless fn is 0, 5 or 10. */
+int trax_math_eval(int device, int fn, const float* a, const float* b, float* out, uint64_t n);
+
 /* Threads per block of the pair, prediction and filter kernels (multiples of
  * 32 in [32, 256]; defaults 128, 128, 256).  No counterpart in the reference,
  * whose work-group sizes are fixed per kernel in the run() methods (e.g.

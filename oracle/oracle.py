@@ -267,8 +267,14 @@ def prefix_sum_blelloch(data: np.ndarray, wg: int) -> np.ndarray:
     return a
 
 
+MATH_CODES = {"atan2": 0, "acos": 1, "atan": 2, "asinh": 3, "log": 4, "div": 5, "sqrt": 6, "floor": 7,
+              "f2u_sat": 8, "f2i_sat": 9}
+
+
 def math_eval(fn: str, a: np.ndarray, b: Optional[np.ndarray] = None) -> np.ndarray:
-    code = {"atan2": 0, "acos": 1, "atan": 2, "asinh": 3, "log": 4}[fn]
+    """trax_math.h's `fn` on the CPU; f2u_sat / f2i_sat results come back as the
+    integers' bits in a float32 array (view them as uint32 / int32)."""
+    code = MATH_CODES[fn]
     a = np.ascontiguousarray(a, dtype=np.float32)
     b = np.ascontiguousarray(b if b is not None else a, dtype=np.float32)
     out = np.zeros_like(a)

@@ -1323,6 +1323,19 @@ void oracle_math_eval(int fn, const float* a, const float* b, float* out, uint64
       case 2: out[i] = trax::atan_(a[i]); break;
       case 3: out[i] = trax::asinh_(a[i]); break;
       case 4: out[i] = trax::log_(a[i]); break;
+      case 5: out[i] = trax::div_(a[i], b[i]); break;
+      case 6: out[i] = trax::sqrt_(a[i]); break;
+      case 7: out[i] = trax::floor_(a[i]); break;
+      case 8: {  // the integer result's bits
+        const uint32_t u = trax::f2u_sat(a[i]);
+        memcpy(&out[i], &u, 4);
+        break;
+      }
+      case 9: {
+        const int32_t v = trax::f2i_sat(a[i]);
+        memcpy(&out[i], &v, 4);
+        break;
+      }
       default: out[i] = 0.0f;
     }
   }

@@ -22,7 +22,7 @@ OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_NAME = "libtrax_gb300.so"
 LIB_PATH = os.path.join(LIB_DIR, LIB_NAME)
 
-SOURCES = ["k_scan.cu", "k_grid.cu", "k_pairs.cu", "k_triplets.cu", "k_link.cu", "capi.cu", "tune.cu", "k_fit.cu", "host_events.cpp", "k_events.cu", "k_tracks.cu"]
+SOURCES = ["k_scan.cu", "k_grid.cu", "k_pairs.cu", "k_triplets.cu", "k_link.cu", "capi.cu", "tune.cu", "k_fit.cu", "host_events.cpp", "k_events.cu", "k_tracks.cu", "k_math.cu"]
 HEADERS = ["trax_device.cuh", "trax_kernels.h", "trax_math.h", "trax_math_coeffs.h", "trax_stages.cuh",
            "trax_lookback.cuh", "trax_events.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -36,7 +36,7 @@ EXPORTED = [
     "trax_physics_triplets", "trax_physics_tracks", "trax_geometry_from_files", "trax_host_alloc",
     "trax_host_free", "trax_set_wait_limit", "trax_debug_skip_publish", "trax_noalloc_set_wait",
     "trax_circle_fit_on", "trax_get_pt", "trax_cellular_automaton_on", "trax_set_pairs_per_thread",
-    "trax_get_pairs_per_thread",
+    "trax_get_pairs_per_thread", "trax_math_eval",
 ]
 
 
@@ -132,6 +132,7 @@ def load() -> ctypes.CDLL:
             "trax_cellular_automaton_on": ([vp, vp, vp, u64, vp, u64, pu64], i32),
             "trax_debug_skip_publish": ([vp, u32], i32),
             "trax_noalloc_set_wait": ([u32, u32], i32),
+            "trax_math_eval": ([i32, i32, vp, vp, vp, u64], i32),
             "trax_seed_batch": ([vp, vp, vp], i32),
             "trax_get_stats": ([vp, vp], i32),
             "trax_get_timings": ([vp, vp, vp], i32),
@@ -170,6 +171,25 @@ def load() -> ctypes.CDLL:
             f.restype = res
         _lib = L
         return L
+
+
+MATH_CODES = {"atan2": 0, "acos": 1, "atan": 2, "asinh": 3, "log": 4, "div": 5, "sqrt": 6, "floor": 7,
+              "f2u_sat": 8, "f2i_sat": 9, "cuda_atan2f": 10, "cuda_acosf": 11, "cuda_atanf": 12,
+              "cuda_asinhf": 13, "cuda_logf": 14}
+
+
+def math_eval(fn: str, a: np.ndarray, b: Optional[np.ndarray] = None, device: int = 0) -> np.ndarray:
+    """trax_math_eval: the library's math (or CUDA's own, "cuda_*") on the
+    device; f2u_sat / f2i_sat results come back as the integers' bits in a
+    float32 array."""
+    L = load()
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = None if b is None else np.ascontiguousarray(b, dtype=np.float32)
+    out = np.zeros_like(a)
+    rc = L.trax_math_eval(device, MATH_CODES[fn], _p(a), _p(b), _p(out), a.size)
+    if rc != 0:
+        raise TraxError(rc, f"trax_math_eval({fn}) failed")
+    return out
 
 
 def pinned_empty(shape, dtype) -> np.ndarray:

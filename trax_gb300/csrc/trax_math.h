@@ -28,7 +28,8 @@
 //            log(2|x|) for |x| > 2^12.
 // Multi-part constants (pi = PI_HI + PI_LO) keep the final additions within
 // about one ulp.  Accuracy is tested against float64 (tests/test_math.py) and
-// against CUDA's own atan2f/acosf/atanf/asinhf on the GPU.
+// against CUDA's own atan2f/acosf/atanf/asinhf on the GPU, where the device
+// build must also give the CPU build's bits (tests/test_gpu_math.py).
 //
 // The header also restates, with fixed semantics, the OpenCL C built-ins the
 // reference kernels use (sign, max, normalize, cross, float->integer
@@ -123,18 +124,29 @@ TRAX_HD float div_(float a, float b) {
 // C/C++ leave out-of-range and NaN conversions undefined and OpenCL leaves
 // them implementation-defined.  Both sides use this saturating definition:
 // truncate toward zero, NaN -> 0, clamp to the destination range.
+// On the device this is one conversion instruction: PTX's cvt.rzi from
+// f32 to an integer type truncates, clamps to the destination range and
+// turns NaN into 0.  tests/test_gpu_math.py holds the two builds equal.
 TRAX_HD uint32_t f2u_sat(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2uint_rz(x);
+#else
   if (!(x > -1.0f)) return 0u;                  // NaN, -inf and x <= -1
   if (x >= 4294967296.0f) return 0xffffffffu;
   if (x < 1.0f) return 0u;                       // (-1, 1) truncates to 0
   return (uint32_t)x;
+#endif
 }
 
 TRAX_HD int32_t f2i_sat(float x) {
+#if defined(__CUDA_ARCH__)
+  return __float2int_rz(x);
+#else
   if (is_nan(x)) return 0;
   if (x >= 2147483648.0f) return 2147483647;
   if (x <= -2147483648.0f) return (int32_t)(-2147483647 - 1);
   return (int32_t)x;
+#endif
 }
 
 // ------------------------------------------------------ OpenCL restatements
