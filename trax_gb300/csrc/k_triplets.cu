@@ -59,27 +59,22 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
       const uint32_t lt = hitLayer[pr.x] - 1;  // Q7
       const uint32_t layer = cfg.layer3[lt] - 1;
       const uint32_t* lG3 = grid + ((size_t)event * cfg.L + layer) * cfg.C;
-      const PredWindow w = pred_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
-      // One walk over the union of both variants' z rows: the phi test is
-      // common, the z test and the row range differ.  Each variant's valid
+      const PredUnionWindow w = pred_union_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
+      // One walk over the union of both variants' z rows with each
+      // variant's own z test (pred_union_window: a hit outside a variant's
+      // rows fails its test); the phi test is common.  Each variant's valid
       // hits come out in its own visit order.
       const uint32_t C = cfg.C, nP = cfg.nP;
       uint32_t* slot = keep + (size_t)gid * TRAX_PRED_KEEP;
       uint32_t nStore = 0;
-      const uint32_t zLo = min(w.zLoSec[0], w.zLoSec[1]), zHi = max(w.zHiSec[0], w.zHiSec[1]);
       // The phi test (TripletThetaPhiPredictor.h:211-214) on hit angles
       // from atan2_, which lie in [-pi, pi] or are NaN: the wrapped window's
       // `phi <= pi` and `-pi <= phi` always hold, so it is lo || hi, the
       // plain one lo && hi (NaN fails both, as in the reference's form).
-      // Per row each variant's z interval (empty outside its rows).
-      const float inf = __int_as_float(0x7f800000);
       const bool wrap = w.wrap != 0u;
+      const float zl0 = w.zLow[0], zh0 = w.zHigh[0], zl1 = w.zLow[1], zh1 = w.zHigh[1];
       const float2* zphi = reinterpret_cast<const float2*>(hits) + 1;  // (z, phi) of hit j at zphi[2 j]
-      for (uint32_t zs = zLo; zs < zHi; ++zs) {
-        const bool in0 = zs >= w.zLoSec[0] && zs < w.zHiSec[0];
-        const bool in1 = zs >= w.zLoSec[1] && zs < w.zHiSec[1];
-        const float zl0 = in0 ? w.zLow[0] : inf, zh0 = in0 ? w.zHigh[0] : -inf;
-        const float zl1 = in1 ? w.zLow[1] : inf, zh1 = in1 ? w.zHigh[1] : -inf;
+      for (uint32_t zs = w.zLo; zs < w.zHi; ++zs) {
         uint32_t a[2], b[2];
         pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
 #pragma unroll

@@ -19,9 +19,8 @@ struct PredWindow {
   bool same;                         // both variants give the same window
 };
 
-__device__ __forceinline__ void pred_z_window(const DevConfig& cfg, float p1z, float p2z, float rOrigin,
-                                              float r2t, float tip2, float minR, float maxR, float sigmaZ,
-                                              float& zLow, float& zHigh, uint32_t& lo, uint32_t& hi) {
+__device__ __forceinline__ void pred_z_bounds(float p1z, float p2z, float rOrigin, float r2t, float tip2,
+                                              float minR, float maxR, float sigmaZ, float& zLow, float& zHigh) {
   const float cotTheta = div_(p2z - p1z, r2t - rOrigin);
   float tmp = p1z + (sqrt_(maxR * maxR - tip2) - rOrigin) * cotTheta;
   zLow = p1z + (sqrt_(minR * minR - tip2) - rOrigin) * cotTheta;
@@ -29,8 +28,54 @@ __device__ __forceinline__ void pred_z_window(const DevConfig& cfg, float p1z, f
   zLow = (float)(tmp > zLow) * zLow + (float)(tmp < zLow) * tmp;
   zLow -= sigmaZ;
   zHigh += sigmaZ;
-  lo = (uint32_t)max(f2i_sat(floor_(div_(zLow - cfg.minZ, cfg.sZ))), 0);
-  hi = min(f2u_sat(floor_(div_(zHigh - cfg.minZ, cfg.sZ))) + 1u, cfg.nZ);
+}
+
+// The z rows of a window: its first row, and its last row without the
+// clamp to nZ (0xffffffff when the bound lies beyond 2^32 rows).
+__device__ __forceinline__ uint32_t pred_row_lo(const DevConfig& cfg, float zLow) {
+  return (uint32_t)max(f2i_sat(floor_(div_(zLow - cfg.minZ, cfg.sZ))), 0);
+}
+__device__ __forceinline__ uint32_t pred_row_hi_raw(const DevConfig& cfg, float zHigh) {
+  return f2u_sat(floor_(div_(zHigh - cfg.minZ, cfg.sZ)));
+}
+
+__device__ __forceinline__ void pred_z_window(const DevConfig& cfg, float p1z, float p2z, float rOrigin,
+                                              float r2t, float tip2, float minR, float maxR, float sigmaZ,
+                                              float& zLow, float& zHigh, uint32_t& lo, uint32_t& hi) {
+  pred_z_bounds(p1z, p2z, rOrigin, r2t, tip2, minR, maxR, sigmaZ, zLow, zHigh);
+  lo = pred_row_lo(cfg, zLow);
+  hi = min(pred_row_hi_raw(cfg, zHigh) + 1u, cfg.nZ);
+}
+
+// The phi window of one pair (TripletThetaPhiPredictor.h:151-185).
+__device__ __forceinline__ void pred_phi_window(const DevConfig& cfg, uint32_t lt, uint32_t layer, float4 h1,
+                                                float4 h2, float& phiLowOut, float& phiHighOut, uint32_t& pL,
+                                                uint32_t& pH, uint32_t& wrap) {
+  const float sigmaPhi = cfg.sigmaPhi[lt];
+  const float p1x = h1.x, p1y = h1.y;
+  const float p2x = h2.x, p2y = h2.y;
+  const float phi = h2.w;  // atan2(p2.y, p2.x)
+  float dPhi = phi - h1.w;
+  dPhi += (dPhi > TRAX_PI_F) ? -2 * TRAX_PI_F : (dPhi < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
+  dPhi = fabs_(dPhi);
+  const float dHits = sqrt_((p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
+  const float twoR = 2 * cfg.minRcurv;
+  const float aH = acos_(div_(dHits, twoR));
+  float tmp = fabs_(aH - cfg.acosMaxR[layer]);
+  float phiLow = fabs_(aH - cfg.acosMinR[layer]);
+  dPhi = cl_max(dPhi, cl_max(tmp, phiLow));
+  float phiHigh = phi + dPhi + sigmaPhi;
+  phiLow = phi - dPhi - sigmaPhi;
+  const bool wrapAround = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
+  phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  phiLowOut = phiLow;
+  phiHighOut = phiHigh;
+  pL = f2u_sat(floor_(div_(phiLow - cfg.minPhi, cfg.sP)));
+  pH = min(f2u_sat(floor_(div_(phiHigh - cfg.minPhi, cfg.sP))) + 1u, cfg.nP);
+  wrap = wrapAround ? 1u : 0u;
 }
 
 // h1, h2: (x, y, z, phi) of the pair's hits; layer = third layer (0-based)
@@ -38,7 +83,6 @@ __device__ __forceinline__ PredWindow pred_window(const DevConfig& cfg, uint32_t
                                                   float4 h2) {
   PredWindow w;
   const float sigmaZ = cfg.sigmaZ[lt];
-  const float sigmaPhi = cfg.sigmaPhi[lt];
   const float minR = cfg.minR[layer];
   const float maxR = cfg.maxR[layer];
   const float p1x = h1.x, p1y = h1.y, p1z = h1.z;
@@ -62,28 +106,79 @@ __device__ __forceinline__ PredWindow pred_window(const DevConfig& cfg, uint32_t
     pred_z_window(cfg, p1z, p2z, rOs, r2t, tip2, minR, maxR, sigmaZ, w.zLow[1], w.zHigh[1], w.zLoSec[1],
                   w.zHiSec[1]);
   }
-  const float phi = h2.w;  // atan2(p2.y, p2.x)
-  float dPhi = phi - h1.w;
-  dPhi += (dPhi > TRAX_PI_F) ? -2 * TRAX_PI_F : (dPhi < -TRAX_PI_F) ? 2 * TRAX_PI_F : 0;
-  dPhi = fabs_(dPhi);
-  const float dHits = sqrt_((p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
-  const float twoR = 2 * cfg.minRcurv;
-  const float aH = acos_(div_(dHits, twoR));
-  float tmp = fabs_(aH - cfg.acosMaxR[layer]);
-  float phiLow = fabs_(aH - cfg.acosMinR[layer]);
-  dPhi = cl_max(dPhi, cl_max(tmp, phiLow));
-  float phiHigh = phi + dPhi + sigmaPhi;
-  phiLow = phi - dPhi - sigmaPhi;
-  const bool wrapAround = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
-  phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
-  w.phiLow = phiLow;
-  w.phiHigh = phiHigh;
-  w.pL = f2u_sat(floor_(div_(phiLow - cfg.minPhi, cfg.sP)));
-  w.pH = min(f2u_sat(floor_(div_(phiHigh - cfg.minPhi, cfg.sP))) + 1u, cfg.nP);
-  w.wrap = wrapAround ? 1u : 0u;
+  pred_phi_window(cfg, lt, layer, h1, h2, w.phiLow, w.phiHigh, w.pL, w.pH, w.wrap);
+  return w;
+}
+
+
+// The count pass's window: both variants' z bounds and one row range, the
+// union of their rows.  A hit's row is g(z) = floor(div(z - minZ, sZ)),
+// saturated, and a variant's rows are [g(zLow), g(zHigh) + 1) clamped to
+// [0, nZ): g is monotone, so a hit in the grid that passes a variant's test
+// zLow <= z <= zHigh lies in that variant's rows, and walking the union with
+// each variant's own test changes no outcome and no visit order.  The union
+// of the rows is the rows of [min zLow, max zHigh], two divisions instead of
+// four.  A variant with a NaN bound (its test never passes) or with rows
+// past 2^32 (the reference's hi wraps to 0: no rows) is switched off by the
+// bounds (+inf, -inf); the union is then taken over the other variant.
+struct PredUnionWindow {
+  float zLow[2], zHigh[2];  // [0] count variant, [1] store variant
+  uint32_t zLo, zHi;        // rows of both
+  float phiLow, phiHigh;
+  uint32_t pL, pH, wrap;
+};
+
+__device__ __forceinline__ PredUnionWindow pred_union_window(const DevConfig& cfg, uint32_t lt, uint32_t layer,
+                                                             float4 h1, float4 h2) {
+  PredUnionWindow w;
+  const float sigmaZ = cfg.sigmaZ[lt];
+  const float minR = cfg.minR[layer];
+  const float maxR = cfg.maxR[layer];
+  const float p1x = h1.x, p1y = h1.y, p1z = h1.z;
+  const float p2x = h2.x, p2y = h2.y, p2z = h2.z;
+  float tip2 = p1y * (p2x - p1x) - p1x * (p2y - p1y);
+  tip2 *= tip2;
+  tip2 = div_(tip2, (p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
+  const float rr = p1x * p1x + p1y * p1y;
+  const float rOc = sqrt_(rr - tip2);  // :130-131
+  const float r1 = sqrt_(rr);
+  const float rOs = sqrt_(r1 * r1 - tip2);  // :305-306
+  const float r2t = sqrt_(p2x * p2x + p2y * p2y - tip2);
+  pred_z_bounds(p1z, p2z, rOc, r2t, tip2, minR, maxR, sigmaZ, w.zLow[0], w.zHigh[0]);
+  if (f2bits(rOc) == f2bits(rOs)) {
+    w.zLow[1] = w.zLow[0];
+    w.zHigh[1] = w.zHigh[0];
+  } else {
+    pred_z_bounds(p1z, p2z, rOs, r2t, tip2, minR, maxR, sigmaZ, w.zLow[1], w.zHigh[1]);
+  }
+  const float inf = __int_as_float(0x7f800000);
+  bool on0 = !is_nan(w.zLow[0]) && !is_nan(w.zHigh[0]);
+  bool on1 = !is_nan(w.zLow[1]) && !is_nan(w.zHigh[1]);
+  float zl = on0 ? (on1 ? fminf(w.zLow[0], w.zLow[1]) : w.zLow[0]) : w.zLow[1];
+  float zh = on0 ? (on1 ? fmaxf(w.zHigh[0], w.zHigh[1]) : w.zHigh[0]) : w.zHigh[1];
+  uint32_t hiRaw = pred_row_hi_raw(cfg, zh);
+  if (hiRaw == 0xffffffffu) {  // a variant whose rows wrap: only far outside the grid
+    on0 = on0 && pred_row_hi_raw(cfg, w.zHigh[0]) != 0xffffffffu;
+    on1 = on1 && pred_row_hi_raw(cfg, w.zHigh[1]) != 0xffffffffu;
+    zl = on0 ? (on1 ? fminf(w.zLow[0], w.zLow[1]) : w.zLow[0]) : w.zLow[1];
+    zh = on0 ? (on1 ? fmaxf(w.zHigh[0], w.zHigh[1]) : w.zHigh[0]) : w.zHigh[1];
+    hiRaw = pred_row_hi_raw(cfg, zh);
+  }
+  if (!on0) {
+    w.zLow[0] = inf;
+    w.zHigh[0] = -inf;
+  }
+  if (!on1) {
+    w.zLow[1] = inf;
+    w.zHigh[1] = -inf;
+  }
+  if (on0 || on1) {
+    w.zLo = pred_row_lo(cfg, zl);
+    w.zHi = min(hiRaw + 1u, cfg.nZ);
+  } else {
+    w.zLo = w.zHi = 0u;
+  }
+  pred_phi_window(cfg, lt, layer, h1, h2, w.phiLow, w.phiHigh, w.pL, w.pH, w.wrap);
   return w;
 }
 
@@ -101,7 +196,8 @@ __device__ __forceinline__ bool pred_valid(const PredWindow& w, int v, float4 h)
 // Visit ranges of one z row of the third layer (the reference's j loop with
 // index = j - (j >= zEnd) * len, zEnd being the next row's start -- Q8): the
 // loop visits P1 = [J0, min(end2, zEnd)) and then P2 = [max(J0, zEnd) - len, end2 - len).
-__device__ __forceinline__ void pred_row_parts(const PredWindow& w, const uint32_t* lG, uint32_t C, uint32_t nP,
+template <class Window>  // PredWindow or PredUnionWindow
+__device__ __forceinline__ void pred_row_parts(const Window& w, const uint32_t* lG, uint32_t C, uint32_t nP,
                                                uint32_t zs, uint32_t& a1, uint32_t& b1, uint32_t& a2, uint32_t& b2) {
   const uint32_t row = zs * (nP + 1);
   const uint32_t zStart = cell_at(lG, row, C);
