@@ -69,10 +69,11 @@ __device__ __forceinline__ PairWindow pair_window(const DevConfig& cfg, uint32_t
   float phiLow = phi - dPhi - sigmaPhi;
   phiHigh = phi + dPhi + sigmaPhi;
   const bool wrapAround = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
-  phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  // (float)((x > pi) * 2) * pi is 2 pi (exact) or +0, as a select
+  phiLow -= (phiLow > TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
+  phiLow += (phiLow < -TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
+  phiHigh -= (phiHigh > TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
+  phiHigh += (phiHigh < -TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
   w.pL = f2u_sat(floor_(div_(phiLow - cfg.minPhi, cfg.sP)));
   w.pH = f2u_sat(floor_(div_(phiHigh - cfg.minPhi, cfg.sP)) + 1);
   w.zLow = zLow;

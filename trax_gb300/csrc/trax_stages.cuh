@@ -67,10 +67,11 @@ __device__ __forceinline__ void pred_phi_window(const DevConfig& cfg, uint32_t l
   float phiHigh = phi + dPhi + sigmaPhi;
   phiLow = phi - dPhi - sigmaPhi;
   const bool wrapAround = phiLow < -TRAX_PI_F || phiHigh > TRAX_PI_F || phiLow > TRAX_PI_F || phiHigh < -TRAX_PI_F;
-  phiLow -= (float)((phiLow > TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiLow += (float)((phiLow < -TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiHigh -= (float)((phiHigh > TRAX_PI_F) * 2) * TRAX_PI_F;
-  phiHigh += (float)((phiHigh < -TRAX_PI_F) * 2) * TRAX_PI_F;
+  // (float)((x > pi) * 2) * pi is 2 pi (exact) or +0, as a select
+  phiLow -= (phiLow > TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
+  phiLow += (phiLow < -TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
+  phiHigh -= (phiHigh > TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
+  phiHigh += (phiHigh < -TRAX_PI_F) ? 2.0f * TRAX_PI_F : 0.0f;
   phiLowOut = phiLow;
   phiHighOut = phiHigh;
   pL = f2u_sat(floor_(div_(phiLow - cfg.minPhi, cfg.sP)));
@@ -144,13 +145,10 @@ __device__ __forceinline__ PredUnionWindow pred_union_window(const DevConfig& cf
   const float r1 = sqrt_(rr);
   const float rOs = sqrt_(r1 * r1 - tip2);  // :305-306
   const float r2t = sqrt_(p2x * p2x + p2y * p2y - tip2);
+  // both variants for every pair: with rOs == rOc the same operations give
+  // the same bounds, and no branch splits the warp
   pred_z_bounds(p1z, p2z, rOc, r2t, tip2, minR, maxR, sigmaZ, w.zLow[0], w.zHigh[0]);
-  if (f2bits(rOc) == f2bits(rOs)) {
-    w.zLow[1] = w.zLow[0];
-    w.zHigh[1] = w.zHigh[0];
-  } else {
-    pred_z_bounds(p1z, p2z, rOs, r2t, tip2, minR, maxR, sigmaZ, w.zLow[1], w.zHigh[1]);
-  }
+  pred_z_bounds(p1z, p2z, rOs, r2t, tip2, minR, maxR, sigmaZ, w.zLow[1], w.zHigh[1]);
   const float inf = __int_as_float(0x7f800000);
   bool on0 = !is_nan(w.zLow[0]) && !is_nan(w.zHigh[0]);
   bool on1 = !is_nan(w.zLow[1]) && !is_nan(w.zHigh[1]);
