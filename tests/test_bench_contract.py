@@ -31,9 +31,12 @@ def test_per_unit_tables_are_keyed_by_grid():
     sys.path.insert(0, REPO)
     import bench
     st = types.SimpleNamespace(n_pairs=1000, n_candidates=500)
-    assert bench.kernel_traffic("predict_count", st, 0, "250x48") == int(32.6 * 1000)
+    per_pair = bench.TRAFFIC_PER_UNIT["250x48"]["predict_count"][1]
+    assert 17.4 <= per_pair < 40  # at least the algorithmic bytes per pair
+    assert bench.kernel_traffic("predict_count", st, 0, "250x48") == int(per_pair * 1000)
     assert bench.kernel_traffic("filter", st, 0, "150x64") == int(27.3 * 500)
     assert bench.kernel_traffic("predict_count", st, 0, "123x45") is None
     assert bench.kernel_traffic("pair_store", st, 0, "250x48") is None
-    for grid in bench.TRAFFIC_PER_UNIT:
-        assert grid in bench.INST_PER_UNIT, grid
+    # instruction counts only where the current prediction kernel was captured:
+    # the workload's own grid
+    assert set(bench.INST_PER_UNIT) <= set(bench.TRAFFIC_PER_UNIT) and "250x48" in bench.INST_PER_UNIT

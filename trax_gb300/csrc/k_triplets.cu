@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
     const uint32_t lt = hitLayer[pr.x] - 1;
     const uint32_t layer = cfg.layer3[lt] - 1;
     const uint32_t* lG3 = grid + ((size_t)event * cfg.L + layer) * cfg.C;
-    const PredWindow w = pred_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
+    const PredWindow w = pred_store_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
     uint32_t n = 0;
     const uint32_t C = cfg.C, nP = cfg.nP;
     for (uint32_t zs = w.zLoSec[1]; zs < w.zHiSec[1] && n < limit; ++zs) {

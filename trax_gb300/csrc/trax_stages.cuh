@@ -111,6 +111,30 @@ __device__ __forceinline__ PredWindow pred_window(const DevConfig& cfg, uint32_t
   return w;
 }
 
+// The store variant alone (predictStore, TripletThetaPhiPredictor.h:286-355:
+// rOrigin = sqrt(sqrt(x^2+y^2)^2 - tip2)), for the store pass's re-walks;
+// both entries of the window hold it.
+__device__ __forceinline__ PredWindow pred_store_window(const DevConfig& cfg, uint32_t lt, uint32_t layer,
+                                                        float4 h1, float4 h2) {
+  PredWindow w;
+  const float p1x = h1.x, p1y = h1.y, p1z = h1.z;
+  const float p2x = h2.x, p2y = h2.y, p2z = h2.z;
+  float tip2 = p1y * (p2x - p1x) - p1x * (p2y - p1y);
+  tip2 *= tip2;
+  tip2 = div_(tip2, (p2x - p1x) * (p2x - p1x) + (p2y - p1y) * (p2y - p1y));
+  const float r1 = sqrt_(p1x * p1x + p1y * p1y);
+  const float rOs = sqrt_(r1 * r1 - tip2);
+  const float r2t = sqrt_(p2x * p2x + p2y * p2y - tip2);
+  pred_z_window(cfg, p1z, p2z, rOs, r2t, tip2, cfg.minR[layer], cfg.maxR[layer], cfg.sigmaZ[lt], w.zLow[1],
+                w.zHigh[1], w.zLoSec[1], w.zHiSec[1]);
+  w.zLow[0] = w.zLow[1];
+  w.zHigh[0] = w.zHigh[1];
+  w.zLoSec[0] = w.zLoSec[1];
+  w.zHiSec[0] = w.zHiSec[1];
+  w.same = true;
+  pred_phi_window(cfg, lt, layer, h1, h2, w.phiLow, w.phiHigh, w.pL, w.pH, w.wrap);
+  return w;
+}
 
 // The count pass's window: both variants' z bounds and one row range, the
 // union of their rows.  A hit's row is g(z) = floor(div(z - minZ, sZ)),
