@@ -204,7 +204,10 @@ int trax_prefix_sum(trax_ctx* ctx, uint32_t* data, uint64_t n);
  *   - Every call looks up the array's device address in the current context
  *     (cudaGetSymbolAddress), so a device reset or another current context
  *     is picked up.  The first call in a context also loads the library's
- *     device code there: make that first call before any stream capture.
+ *     device code there.
+ *   - No call can be captured into a CUDA graph: each one synchronises
+ *     `stream` and reads the error word back (below), which a capturing
+ *     stream refuses, invalidating the capture.
  *   - All calls share the array and each call clears what it uses; calls
  *     whose work overlaps on the GPU (other streams, other host threads) race.
  *   - Before returning, the call copies the scan's error word to the host and
