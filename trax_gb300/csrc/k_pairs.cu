@@ -104,6 +104,17 @@ __device__ __forceinline__ bool pair_ok(const PairTest& t, float2 h) {
   return t.zl <= h.x && h.x <= t.zh && ((t.a1 <= h.y && h.y <= t.b1) || (t.a2 <= h.y && h.y <= t.b2));
 }
 
+// The count pass's form of the window test (PairGeneratorBeamspot.h:192,
+// :212-214).  The hits' angles come from atan2_ and lie in [-pi, pi] or are
+// NaN, so a wrapped window's `phi <= pi` and `-pi <= phi` always hold: its
+// phi test is lo || hi, a plain window's lo && hi (NaN fails both, as in the
+// reference's form).  The store pass keeps the forms below, which measured
+// faster there.
+__device__ __forceinline__ bool pair_count_ok(const PairWindow& w, float4 h) {
+  const bool lo = w.phiLow <= h.w, hi = h.w <= w.phiHigh;
+  return w.zLow <= h.z && h.z <= w.zHigh && (w.wrap ? (lo || hi) : (lo && hi));
+}
+
 __device__ __forceinline__ bool pair_valid(const PairWindow& w, float4 h) {
   bool valid = w.zLow <= h.z && h.z <= w.zHigh;
   const float actPhi = h.w;
@@ -232,8 +243,8 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
         uint32_t a1, b1, a2, b2;
         pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
         if (simple) simple = rows_in_order(a1, b1, a2, b2, prevEnd);
-        for (uint32_t j = a1; j < b1; ++j) nFound += pair_valid(w, hits[j]);
-        for (uint32_t j = a2; j < b2; ++j) nFound += pair_valid(w, hits[j]);
+        for (uint32_t j = a1; j < b1; ++j) nFound += pair_count_ok(w, hits[j]);
+        for (uint32_t j = a2; j < b2; ++j) nFound += pair_count_ok(w, hits[j]);
       }
       taskCount[k] = nFound;
       state.bounds[k] = make_float4(w.zLow, w.zHigh, w.phiLow, w.phiHigh);
