@@ -171,18 +171,42 @@ CPU_KIND_NOTE = {
 }
 
 
-def cpu_baseline(batch, n_events: int):
+def host_cpu() -> dict:
+    """The host's processor: logical CPUs, architecture and model name."""
+    import platform
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"logical_cpus": os.cpu_count() or 1, "machine": platform.machine(), "model": model}
+
+
+def cpu_baseline(batch, n_events: int, single_events: int = 8):
     sample = batch.subset(range(min(n_events, batch.n_events)))
     cores = os.cpu_count() or 1
     kind = cpu_engine()
     t0 = time.perf_counter()
     trip = cpu_run(sample, cores, kind)
     dt = time.perf_counter() - t0
+    # the same path on one host thread, over the first few events
+    one = batch.subset(range(min(single_events, batch.n_events)))
+    t1 = time.perf_counter()
+    trip1 = cpu_run(one, 1, kind)
+    dt1 = time.perf_counter() - t1
     return {"value": round(sample.n_events / dt, 3), "unit": "events/s", "cores": cores, "kind": kind,
             "sample": f"first {sample.n_events} events of the 1000-event workload at the same grid "
                       f"({batch.n_z}x{batch.n_phi}), one event per group, {cores} host threads, {dt:.2f} s wall; "
                       + CPU_KIND_NOTE[kind],
-            "triplets_per_s": round(trip / dt, 1)}
+            "triplets_per_s": round(trip / dt, 1),
+            "single_thread": {"value": round(one.n_events / dt1, 3), "unit": "events/s",
+                              "triplets_per_s": round(trip1 / dt1, 1),
+                              "sample": f"first {one.n_events} events, one host thread, {dt1:.2f} s wall"},
+            "host": host_cpu()}
 
 
 def peaks():
@@ -708,7 +732,7 @@ def run_reference(args, ranks):
         "cpu_baseline": {"value": v, "unit": "events/s", "cores": cores, "kind": kind,
                          "sample": f"{per_step} events per step of the 1000-event workload (rotating windows) at "
                                    f"grid {batch.n_z}x{batch.n_phi}, one event per group, {cores} host threads; "
-                                   + CPU_KIND_NOTE[kind]},
+                                   + CPU_KIND_NOTE[kind], "host": host_cpu()},
         "e2e": {"value": v, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
