@@ -220,6 +220,21 @@ TRAX_HD float atan_pos(float a) {
   return atan_kernel(a);
 }
 
+// atan_pos without branches, for callers whose neighbouring lanes fall in
+// different intervals (atan2 of arbitrary directions): the interval selects
+// the operands of one division and the constants around one polynomial.
+// Every lane performs the operations of atan_pos above (a / 1 == a), so the
+// result is the same.
+TRAX_HD float atan_pos_select(float a) {
+  const bool big = a > TRAX_TAN_3PI_8;
+  const bool mid = !big && a > TRAX_TAN_PI_8;
+  const float t = div_(big ? -1.0f : (mid ? a - 1.0f : a), big ? a : (mid ? a + 1.0f : 1.0f));
+  const float p = atan_kernel(t);
+  const float hi = big ? TRAX_PIO2_HI : TRAX_PIO4_HI;
+  const float lo = big ? TRAX_PIO2_LO : TRAX_PIO4_LO;
+  return (big || mid) ? hi + (p + lo) : p;
+}
+
 TRAX_HD float atan_(float x) {
   if (is_nan(x)) return x;
   float r = atan_pos(fabs_(x));
@@ -247,11 +262,11 @@ TRAX_HD float atan2_(float y, float x) {
   if (is_inf(ay) || ax == 0.0f) {
     return copysign_(TRAX_PIO2_HI, y);
   }
-  if (ay <= ax) {
-    r = atan_pos(div_(ay, ax));  // [0, pi/4]
-  } else {
-    r = TRAX_PIO2_HI - (atan_pos(div_(ax, ay)) - TRAX_PIO2_LO);  // (pi/4, pi/2)
-  }
+  // [0, pi/4] from atan(ay / ax), (pi/4, pi/2) as pi/2 - atan(ax / ay): one
+  // division and one atan_pos_select for either half
+  const bool lower = ay <= ax;
+  const float rp = atan_pos_select(div_(lower ? ay : ax, lower ? ax : ay));
+  r = lower ? rp : TRAX_PIO2_HI - (rp - TRAX_PIO2_LO);
   if (sign_bit(x)) {
     r = TRAX_PI_F - (r - TRAX_PI_LO);
   }
