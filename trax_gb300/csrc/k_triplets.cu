@@ -38,9 +38,8 @@ int grid_for(uint64_t items, int threads) {
 // exclusive offsets within the warp to candCount and the warp's sum to
 // warpSums; only those sums (one per 32 pairs) are then scanned, and a
 // pair's position is its warp's scanned sum plus its offset in the warp.
-// At most 40 registers (six blocks of 256 threads per SM): the occupancy
-// gained outweighs the few spilled bytes (3.20 -> 3.13 ms on the
-// 1000-event batch).
+// At most 40 registers (six blocks of 256 threads per SM), where it spills
+// nothing; 32 registers (eight blocks) spill and measured slower, as did 48.
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
     predict_count_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
