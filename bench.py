@@ -462,6 +462,8 @@ def run_config3(device: int, steps: int):
                                            "host-synced run and captures the graph; replays recapture only after "
                                            "a capacity overflow"},
                 "kernel_launches_per_step": st.kernel_launches,
+                "candidate_slots": ctx.candidate_slots(),
+                "kernel_ms": {k: round(v, 3) for k, v in ctx.timings()[1].items() if v >= 0},
                 "parity": "tests/test_gpu_parity.py::test_pileup_workload_at_full_size: every array equals the "
                           "oracle run on the whole batch"}
     finally:
@@ -550,6 +552,7 @@ def run_ours(args, ranks):
                    "events_per_gpu": batch.n_events, "hits_per_gpu": n_hits, "grid": f"{batch.n_z}x{batch.n_phi}",
                    "block_sizes": {k: shape[k] for k in ("pair_threads", "predict_threads", "filter_threads")},
                    "predict_pairs_per_thread": ctx.pairs_per_thread(),
+                   "predict_candidate_slots": ctx.candidate_slots(),
                    "autotune": None if tune is None else {
                        "shapes_timed": tune["shapes_timed"], "from_cache": bool(tune["from_cache"]),
                        "best_ms": round(tune["best_ms"], 4), "default_shape_ms": round(tune["default_ms"], 4)},
@@ -629,6 +632,7 @@ def run_ours(args, ranks):
             c2.set_block_sizes(shape_now["pair_threads"], shape_now["predict_threads"],
                                shape_now["filter_threads"])
             c2.set_pairs_per_thread(ctx.pairs_per_thread())
+            c2.set_candidate_slots(tune["candidate_slots"] if tune else 0)
             for _w in range(2):
                 c2.seed_batch(use_graph=True)
             outs = ([capi.pinned_empty((max(st.n_triplets, 1),), np.uint32) for _ in range(3)]

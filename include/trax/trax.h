@@ -264,6 +264,17 @@ int trax_get_launch_config(trax_ctx* ctx, uint32_t* out5);
  * tunes it after the block sizes. */
 int trax_set_pairs_per_thread(trax_ctx* ctx, uint32_t k);
 int trax_get_pairs_per_thread(trax_ctx* ctx, uint32_t* k);
+/* Candidates the prediction's count pass captures per pair for its store
+ * pass: 4, 8, 16 or 32, or 0 for automatic (the default): after each
+ * calibration of trax_seed_batch the library takes 4, 8, 16 or 32 from the
+ * batch's mean candidates per pair (up to 1, 2.5, 6, above).  A pair with
+ * more candidates than slots is walked again by the store pass; more slots
+ * cost the pairs with few candidates more scattered writes and reads.  The
+ * results do not change.  The reference's predictStore walks every pair
+ * again (TripletThetaPhiPredictor.h:232-447).  get returns the number in
+ * effect; trax_autotune tunes it after the pairs per thread. */
+int trax_set_candidate_slots(trax_ctx* ctx, uint32_t k);
+int trax_get_candidate_slots(trax_ctx* ctx, uint32_t* k);
 
 /* ------------------------------------------------------------- batched
  * The whole chain (buildTriplets, TripletBuilder.cpp:312-467) for all
@@ -294,6 +305,7 @@ typedef struct trax_tune_result {
   uint32_t from_cache;       /* 1: taken from the cache file */
   uint32_t shapes_timed;     /* shapes timed by this call */
   uint32_t pairs_per_thread; /* of the prediction count (trax_set_pairs_per_thread) */
+  uint32_t candidate_slots;  /* trax_set_candidate_slots: 0 = the library's choice */
   double best_ms;            /* device time of one chain replay at the chosen shape */
   double default_ms;         /* the same for the shape the context had before */
 } trax_tune_result;

@@ -65,6 +65,35 @@ def test_pairs_per_thread_keep_results(ctx, oracle_lib, k):
         ctx.set_block_sizes(128, 128, 256)
 
 
+@pytest.mark.parametrize("workload", ["ttbar", "pileup"])
+def test_candidate_slots_keep_results(ctx, oracle_lib, trax_lib, workload):
+    """Any number of captured candidates per pair (the store pass copies them,
+    and walks again the pairs with more) gives the same candidates; the
+    automatic choice follows the batch's candidates per pair."""
+    import dataclasses
+    if workload == "ttbar":
+        batch = events.generate(2, n_events=12)
+    else:  # many candidates per pair: most pairs have more than 4
+        batch = events.generate_workload(dataclasses.replace(events.workload(3), n_events=1, n_vertices=6))
+    ref = oracle_lib.run(batch)[0]
+    ctx.upload(batch)
+    try:
+        for k in [4, 8, 16, 32, 0]:
+            ctx.set_candidate_slots(k)
+            ctx.seed_batch(use_graph=True)
+            compare(ctx.results(), ref)
+            if k:
+                assert ctx.candidate_slots() == k
+        st = ctx.stats()
+        per_pair = st.n_candidates / max(st.n_pairs, 1)
+        want = 4 if per_pair <= 1 else 8 if per_pair <= 2.5 else 16 if per_pair <= 6 else 32
+        assert ctx.candidate_slots() == want, (per_pair, ctx.candidate_slots())
+        with pytest.raises(trax_lib.TraxError):
+            ctx.set_candidate_slots(12)
+    finally:
+        ctx.set_candidate_slots(0)
+
+
 def test_invalid_block_sizes_rejected(ctx, trax_lib):
     for bad in [(0, 128, 128), (33, 128, 128), (128, 512, 128), (128, 128, 16)]:
         with pytest.raises(trax_lib.TraxError) as e:
@@ -93,6 +122,8 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
         entries = json.loads(cache.read_text())["entries"]
         assert len(entries) == 1 and entries[0]["n_z"] == res["n_z"] and entries[0]["sm_count"] > 0
         assert entries[0]["pairs_per_thread"] == res["pairs_per_thread"]
+        assert res["candidate_slots"] in (0, 4, 8, 16, 32)
+        assert entries[0]["candidate_slots"] == res["candidate_slots"]
     finally:
         c.close()
     # a new context with the same workload takes the cached shape without timing
@@ -101,7 +132,8 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
         c.upload(events.generate(1, n_events=20))
         res2 = c.autotune(cache_path=str(cache), search_grid=True, replays=1)
         assert res2["from_cache"] == 1 and res2["shapes_timed"] == 0
-        keys = ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "pairs_per_thread")
+        keys = ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "pairs_per_thread",
+                "candidate_slots")
         assert [res2[k] for k in keys] == [res[k] for k in keys]
         # a different workload gets its own entry
         c.upload(events.generate(1, n_events=21))
@@ -113,7 +145,8 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
 
 
 def test_autotune_cache_entry_without_pairs_per_thread(trax_lib, tmp_path):
-    """Cache files written before the pairs-per-thread axis existed still load (as 1)."""
+    """Cache files written before the pairs-per-thread and candidate-slot axes
+    existed still load (as 1 and the library's own choice)."""
     batch = events.generate(1, n_events=20)
     cache = tmp_path / "tune.json"
     c = trax_lib.Context(0)
@@ -123,9 +156,12 @@ def test_autotune_cache_entry_without_pairs_per_thread(trax_lib, tmp_path):
         doc = json.loads(cache.read_text())
         for e in doc["entries"]:
             e.pop("pairs_per_thread")
+            e.pop("candidate_slots")
         cache.write_text(json.dumps(doc))
         c.set_pairs_per_thread(4)
+        c.set_candidate_slots(32)
         res = c.autotune(cache_path=str(cache), search_grid=False, replays=1)
         assert res["from_cache"] == 1 and res["pairs_per_thread"] == 1 and c.pairs_per_thread() == 1
+        assert res["candidate_slots"] == 0
     finally:
         c.close()

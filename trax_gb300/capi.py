@@ -36,7 +36,7 @@ EXPORTED = [
     "trax_physics_triplets", "trax_physics_tracks", "trax_geometry_from_files", "trax_host_alloc",
     "trax_host_free", "trax_set_wait_limit", "trax_debug_skip_publish", "trax_noalloc_set_wait",
     "trax_circle_fit_on", "trax_get_pt", "trax_cellular_automaton_on", "trax_set_pairs_per_thread",
-    "trax_get_pairs_per_thread", "trax_math_eval",
+    "trax_get_pairs_per_thread", "trax_math_eval", "trax_set_candidate_slots", "trax_get_candidate_slots",
 ]
 
 
@@ -82,7 +82,7 @@ class TuneOptsC(ctypes.Structure):
 class TuneResultC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint32) for n in (
         "n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "from_cache", "shapes_timed",
-        "pairs_per_thread")] + [
+        "pairs_per_thread", "candidate_slots")] + [
         ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
 
 
@@ -126,6 +126,8 @@ def load() -> ctypes.CDLL:
             "trax_prefix_sum": ([vp, vp, u64], i32),
             "trax_set_pairs_per_thread": ([vp, u32], i32),
             "trax_get_pairs_per_thread": ([vp, vp], i32),
+            "trax_set_candidate_slots": ([vp, u32], i32),
+            "trax_get_candidate_slots": ([vp, vp], i32),
             "trax_set_wait_limit": ([vp, u32], i32),
             "trax_circle_fit_on": ([vp, vp, u64], i32),
             "trax_get_pt": ([vp, vp], i32),
@@ -368,6 +370,16 @@ class Context:
     def set_pairs_per_thread(self, k: int):
         """Pairs per thread of the prediction's count pass (1, 2 or 4)."""
         self._check(self._L.trax_set_pairs_per_thread(self._h, k))
+
+    def set_candidate_slots(self, k: int):
+        """Candidates captured per pair by the prediction count (4, 8, 16, 32; 0: automatic)."""
+        self._check(self._L.trax_set_candidate_slots(self._h, k))
+
+    def candidate_slots(self) -> int:
+        """The number of captured candidates per pair in effect."""
+        k = ctypes.c_uint32()
+        self._check(self._L.trax_get_candidate_slots(self._h, ctypes.byref(k)))
+        return int(k.value)
 
     def pairs_per_thread(self) -> int:
         k = ctypes.c_uint32()

@@ -108,6 +108,9 @@ struct trax_ctx {
   uint32_t nZ = 0, nP = 0;
   uint32_t pairThreads = 128, predThreads = 128, filterThreads = 256;  // launch shape
   uint32_t predK = 1;  // pairs per thread of the prediction count pass
+  // candidates the prediction count captures per pair: keepSlots when the
+  // caller set it, else keepAuto, chosen after each calibration
+  uint32_t keepSlots = 0, keepAuto = TRAX_PRED_KEEP;
   bool haveLT = false, haveGeom = false, haveGrid = false, haveHits = false;
   bool cfgDirty = true;  // layer triplets or geometry changed since the device configuration was built
   // batch shape
@@ -304,6 +307,7 @@ int build_config(trax_ctx* c, bool seeding = true) {
   g.predThreads = c->predThreads;
   g.filterThreads = c->filterThreads;
   g.predPairsPerThread = c->predK;
+  g.predKeep = c->keepSlots ? c->keepSlots : c->keepAuto;
   for (uint32_t p = 0; p < g.nLT; ++p) {
     const trax_layer_triplet& t = c->lts[p];
     if (t.layer1 < 1 || t.layer2 < 1 || t.layer3 < 1 || t.layer1 > c->L || t.layer2 > c->L || t.layer3 > c->L)
@@ -474,7 +478,7 @@ int stage_predict(trax_ctx* c, Mode mode) {
   // warp the candidates' sum (scanned into the warp's first position)
   ENSURE(candLocal, maxPairs + 1, 4);
   ENSURE(predWarps, maxWarps + 1, 4);
-  ENSURE(predKeep, maxPairs * TRAX_PRED_KEEP, 4);
+  ENSURE(predKeep, maxPairs * c->cfg.predKeep, 4);
   ENSURE(candOffsets, S + 1, 4);
   uint32_t* candLocal = ptr<uint32_t>(c->candLocal);
   uint32_t* warpSums = ptr<uint32_t>(c->predWarps);
@@ -747,7 +751,7 @@ int size_device_buffers(trax_ctx* c) {
   ENSURE(pairs, c->capPairs, 8);
   ENSURE(candLocal, c->capPairs + 1, 4);
   ENSURE(predWarps, (c->capPairs + 31) / 32 + 1, 4);
-  ENSURE(predKeep, c->capPairs * TRAX_PRED_KEEP, 4);
+  ENSURE(predKeep, c->capPairs * c->cfg.predKeep, 4);
   ENSURE(cands, c->capCands, 8);
   ENSURE(flagWords, (c->capCands + 31) / 32 + 1, 4);
   ENSURE(flagSums, (c->capCands + 31) / 32 + 1, 4);
@@ -772,6 +776,21 @@ void drop_graph(trax_ctx* c) {
   c->graphExec = nullptr;
   c->graph = nullptr;
   c->graphKey = 0;
+}
+
+// Candidates captured per pair when the caller leaves the choice to the
+// library, from the mean candidates per pair m of the calibrated batch: 4
+// up to m = 1, 8 up to 2.5, 16 up to 6, else 32.  More slots spare the
+// store pass its re-walks of pairs with more candidates, and spread the
+// captures of pairs with few over more sectors.  On GB300, at m = 0.5 (1000
+// ttbar-like events) 4 slots are fastest (16: prediction store 0.47 ->
+// 0.65 ms); at m = 4.2 (16 pileup events) 16 slots take the prediction
+// store from 14.8 to 4.3 ms and the chain from 50.6 to 40.4 ms.
+uint32_t auto_keep_slots(uint64_t nCands, uint64_t nPairs) {
+  if (nPairs == 0 || nCands <= nPairs) return 4u;
+  if (2 * nCands <= 5 * nPairs) return 8u;
+  if (nCands <= 6 * nPairs) return 16u;
+  return 32u;
 }
 
 uint64_t shape_key(trax_ctx* c, bool linking) {
@@ -1037,6 +1056,20 @@ int trax_set_pairs_per_thread(trax_ctx* c, uint32_t k) {
   if (!c) return TRAX_ERR_ARG;
   if (k != 1 && k != 2 && k != 4) return fail(c, TRAX_ERR_ARG, "pairs per thread must be 1, 2 or 4");
   c->predK = k;
+  return TRAX_OK;
+}
+
+int trax_set_candidate_slots(trax_ctx* c, uint32_t k) {
+  if (!c) return TRAX_ERR_ARG;
+  if (k != 0 && k != 4 && k != 8 && k != 16 && k != 32)
+    return fail(c, TRAX_ERR_ARG, "candidate slots must be 0 (automatic), 4, 8, 16 or 32");
+  c->keepSlots = k;
+  return TRAX_OK;
+}
+
+int trax_get_candidate_slots(trax_ctx* c, uint32_t* k) {
+  if (!c || !k) return TRAX_ERR_ARG;
+  *k = c->keepSlots ? c->keepSlots : c->keepAuto;
   return TRAX_OK;
 }
 
@@ -1444,6 +1477,10 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
       ++c->graphCaptures;
       drop_graph(c);
       RC(run_synced_chain(c, linking));
+      if (!c->keepSlots) {  // the capture slots for what this batch's pairs hold
+        c->keepAuto = auto_keep_slots(c->nCands, c->nPairs);
+        c->cfg.predKeep = c->keepAuto;
+      }
       RC(size_device_buffers(c));
       c->launches = 0;
       CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));

@@ -30,7 +30,7 @@ int grid_for(uint64_t items, int threads) {
 }
 
 // Count pass (predictCount, :190-219) that also captures the first
-// min(count, TRAX_PRED_KEEP) candidates the store pass would write (the store
+// min(count, cfg.predKeep) candidates the store pass would write (the store
 // variant's valid hits, capped at the count; slots it would leave unwritten
 // get the sentinel), so that the store pass is a copy for most pairs.
 // The prefix sum between predictCount and predictStore is split in two:
@@ -64,7 +64,8 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
       // rows fails its test); the phi test is common.  Each variant's valid
       // hits come out in its own visit order.
       const uint32_t C = cfg.C, nP = cfg.nP;
-      uint32_t* slot = keep + (size_t)gid * TRAX_PRED_KEEP;
+      const uint32_t nKeep = cfg.predKeep;
+      uint32_t* slot = keep + (size_t)gid * nKeep;
       uint32_t nStore = 0;
       // The phi test (TripletThetaPhiPredictor.h:211-214) on hit angles
       // from atan2_, which lie in [-pi, pi] or are NaN: the wrapped window's
@@ -85,7 +86,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
             const bool phiOk = wrap ? (lo || hi) : (lo && hi);
             count += (phiOk && zl0 <= h.x && h.x <= zh0);
             if (phiOk && zl1 <= h.x && h.x <= zh1) {
-              if (nStore < TRAX_PRED_KEEP) slot[nStore] = j;
+              if (nStore < nKeep) slot[nStore] = j;
               ++nStore;
             }
           }
@@ -93,7 +94,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
       }
       // the store pass writes at most `count` candidates; missing ones are
       // slots the reference leaves unwritten
-      const uint32_t k = min(count, (uint32_t)TRAX_PRED_KEEP);
+      const uint32_t k = min(count, nKeep);
       for (uint32_t q = nStore; q < k; ++q) slot[q] = TRAX_SENTINEL;
     }
     uint32_t incl = count;
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
         } else {
           if (k >= 0) {
             // the pair's end: store-pass slots past the valid hits get the sentinel
-            const uint32_t kk = min(cnt, (uint32_t)TRAX_PRED_KEEP);
+            const uint32_t kk = min(cnt, cfg.predKeep);
             for (uint32_t q = nStore; q < kk; ++q) slot[q] = TRAX_SENTINEL;
 #pragma unroll
             for (int q = 0; q < K; ++q)
@@ -239,7 +240,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
             pa2 = rw.wrap ? -TRAX_PI_F : inf;
             pb2 = rw.wrap ? ps.phiHigh : -inf;
             lG3 = grid + ps.gridOff;
-            slot = keep + (size_t)(base + 32u * k + lane) * TRAX_PRED_KEEP;
+            slot = keep + (size_t)(base + 32u * k + lane) * cfg.predKeep;
             zs = min(zlo[0], zlo[1]);
             zHi = max(zhi[0], zhi[1]);
             if (zs < zHi) break;
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
         const bool phiOk = (pa1 <= h.y && h.y <= pb1) || (pa2 <= h.y && h.y <= pb2);
         cnt += (phiOk && zl0 <= h.x && h.x <= zh0);
         if (phiOk && zl1 <= h.x && h.x <= zh1) {
-          if (nStore < TRAX_PRED_KEEP) slot[nStore] = j;
+          if (nStore < cfg.predKeep) slot[nStore] = j;
           ++nStore;
         }
         if (++j >= end) live = advance();
@@ -327,8 +328,8 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
     else if (limit > capCands - pos) limit = capCands - pos;
     if (limit == 0) continue;
     uint2* out = cands + pos;
-    if (limit <= (uint32_t)TRAX_PRED_KEEP) {
-      const uint32_t* slot = keep + (size_t)gid * TRAX_PRED_KEEP;
+    if (limit <= cfg.predKeep) {
+      const uint32_t* slot = keep + (size_t)gid * cfg.predKeep;
       for (uint32_t q = 0; q < limit; ++q) {
         const uint32_t h = slot[q];
         sent += h == TRAX_SENTINEL;

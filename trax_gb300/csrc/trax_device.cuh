@@ -38,6 +38,7 @@ struct DevConfig {
   // prediction and filter kernels; at most TRAX_MAX_TUNED_THREADS)
   uint32_t pairThreads, predThreads, filterThreads;
   uint32_t predPairsPerThread;  // 1, 2 or 4 pairs per thread in the prediction count pass
+  uint32_t predKeep;            // candidates captured per pair by the count pass (4, 8, 16 or 32)
 };
 
 #define TRAX_MAX_TUNED_THREADS 256

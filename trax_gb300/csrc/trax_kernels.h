@@ -171,11 +171,13 @@ cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const u
 // Count pass (emit == false): per pair the exclusive offset of its
 // candidates within its warp of 32 pairs (candCount[nPairs]), the sum of
 // each warp's counts in warpSums[ceil(nPairs/32) + 1] (+1 slot zeroed; the
-// number of sums goes to *nWarpsOut) and up to TRAX_PRED_KEEP captured
-// candidates per pair in keep[nPairs * TRAX_PRED_KEEP]; store pass
+// number of sums goes to *nWarpsOut) and up to cfg.predKeep captured
+// candidates per pair in keep[nPairs * cfg.predKeep]; store pass
 // (emit == true): with warpSums exclusively scanned, candidates at
-// warpSums[gid / 32] + candCount[gid].
+// warpSums[gid / 32] + candCount[gid].  predKeep is 4 (TRAX_PRED_KEEP,
+// the default) to TRAX_PRED_KEEP_MAX.
 #define TRAX_PRED_KEEP 4
+#define TRAX_PRED_KEEP_MAX 32
 
 // grids of up to this many cells per layer are built with shared-memory
 // counters (4 bytes per cell)

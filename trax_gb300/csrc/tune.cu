@@ -25,12 +25,14 @@ namespace {
 struct Shape {
   uint32_t nZ, nP, pairT, predT, filtT;
   uint32_t predK;  // pairs per thread of the prediction count
+  uint32_t slots;  // candidates it captures per pair (0: the library's choice)
 };
 
 int apply_shape(trax_ctx* c, const Shape& s) {
   int rc = trax_set_grid(c, s.nZ, s.nP);
   if (rc == TRAX_OK) rc = trax_set_block_sizes(c, s.pairT, s.predT, s.filtT);
   if (rc == TRAX_OK) rc = trax_set_pairs_per_thread(c, s.predK);
+  if (rc == TRAX_OK) rc = trax_set_candidate_slots(c, s.slots);
   return rc;
 }
 
@@ -123,9 +125,11 @@ bool cache_lookup(const char* path, const std::string& key, Shape* s, double* ms
     if (!field_u64(e, "n_z", &v[0]) || !field_u64(e, "n_phi", &v[1]) || !field_u64(e, "pair_threads", &v[2]) ||
         !field_u64(e, "predict_threads", &v[3]) || !field_u64(e, "filter_threads", &v[4]))
       continue;
-    unsigned long long ppt = 1;  // entries written before the axis existed
+    unsigned long long ppt = 1, slots = 0;  // entries written before these axes existed
     field_u64(e, "pairs_per_thread", &ppt);
-    *s = Shape{(uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3], (uint32_t)v[4], (uint32_t)ppt};
+    field_u64(e, "candidate_slots", &slots);
+    *s = Shape{(uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3], (uint32_t)v[4], (uint32_t)ppt,
+               (uint32_t)slots};
     if (!field_f64(e, "ms", ms)) *ms = 0.0;
     return true;
   }
@@ -141,8 +145,9 @@ bool cache_store(const char* path, const std::string& key, int sms, const Shape&
   char b[512];
   snprintf(b, sizeof(b),
            "{\"key\": \"%s\", \"sm_count\": %d, \"n_z\": %u, \"n_phi\": %u, \"pair_threads\": %u, "
-           "\"predict_threads\": %u, \"filter_threads\": %u, \"pairs_per_thread\": %u, \"ms\": %.6f}",
-           key.c_str(), sms, s.nZ, s.nP, s.pairT, s.predT, s.filtT, s.predK, ms);
+           "\"predict_threads\": %u, \"filter_threads\": %u, \"pairs_per_thread\": %u, "
+           "\"candidate_slots\": %u, \"ms\": %.6f}",
+           key.c_str(), sms, s.nZ, s.nP, s.pairT, s.predT, s.filtT, s.predK, s.slots, ms);
   keep.push_back(b);
   const std::string tmp = std::string(path) + ".tmp";
   {
@@ -179,7 +184,8 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
   int rc = trax_get_launch_config(c, cur);
   if (rc == TRAX_OK) rc = trax_get_pairs_per_thread(c, &curK);
   if (rc != TRAX_OK) return rc;
-  const Shape start{cur[0], cur[1], cur[2], cur[3], cur[4], curK};
+  // the capture slots start from the library's own choice
+  const Shape start{cur[0], cur[1], cur[2], cur[3], cur[4], curK, 0u};
 
   uint64_t h = trax::workload_hash(c);
   h ^= (uint64_t)sms * 0x9e3779b97f4a7c15ull;
@@ -220,7 +226,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
         for (uint32_t p : ps) {
           if ((z + 1) * (p + 1) > TRAX_GRID_SMEM_CELLS) continue;
           if (z == start.nZ && p == start.nP) continue;
-          consider(Shape{z, p, best.pairT, best.predT, best.filtT, best.predK});
+          consider(Shape{z, p, best.pairT, best.predT, best.filtT, best.predK, best.slots});
         }
     }
     static const uint32_t ts[] = {64, 96, 128, 192, 256};
@@ -241,6 +247,14 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
       s.predK = k;
       consider(s);
     }
+    // then the candidates captured per pair
+    static const uint32_t slotChoices[] = {4, 8, 16, 32};
+    const Shape byK = best;
+    for (uint32_t k : slotChoices) {
+      Shape s = byK;
+      s.slots = k;
+      consider(s);
+    }
     rc = apply_shape(c, best);
     if (rc != TRAX_OK) return rc;
     res.best_ms = bestMs;
@@ -255,6 +269,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
   res.predict_threads = best.predT;
   res.filter_threads = best.filtT;
   res.pairs_per_thread = best.predK;
+  res.candidate_slots = best.slots;
   if (result) *result = res;
   return TRAX_OK;
 }
