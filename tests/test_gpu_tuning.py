@@ -49,19 +49,22 @@ def test_grid_sizes_around_shared_memory_limit(ctx, oracle_lib, grid):
 def test_pairs_per_thread_keep_results(ctx, oracle_lib, k):
     """The prediction count with K pairs per thread (windows staged in shared
     memory, one flat walk per lane) writes the same counts, offsets and kept
-    candidates as one pair per thread, at several block sizes."""
+    candidates as one pair per thread, at several block sizes and numbers of
+    captured candidates."""
     batch = events.generate(2, n_events=12)
     ref = oracle_lib.run(batch)[0]
     ctx.upload(batch)
     try:
-        for blocks in [(256, 64, 256), (128, 128, 128), (128, 256, 128)]:
+        for blocks, slots in [((256, 64, 256), 0), ((128, 128, 128), 16), ((128, 256, 128), 8)]:
             ctx.set_block_sizes(*blocks)
             ctx.set_pairs_per_thread(k)
+            ctx.set_candidate_slots(slots)
             assert ctx.pairs_per_thread() == k
             ctx.seed_batch(use_graph=True)
             compare(ctx.results(), ref)
     finally:
         ctx.set_pairs_per_thread(1)
+        ctx.set_candidate_slots(0)
         ctx.set_block_sizes(128, 128, 256)
 
 
