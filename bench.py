@@ -260,7 +260,7 @@ TRAFFIC_PER_UNIT = {  # by grid (nZ x nPhi): the grid changes the cells read and
 # 300-event capture / its units): the dominant kernels are issue-bound, so
 # their position against the SMs' issue rate is reported beside the HBM one.
 # Captured for the current prediction kernel at the workload's grid only.
-INST_PER_UNIT = {"250x48": {"predict_count": ("pairs", 23.94)}}
+INST_PER_UNIT = {"250x48": {"predict_count": ("pairs", 24.29)}}
 
 
 def kernel_issue(name, st, ms, clk, device, grid):
