@@ -664,7 +664,10 @@ bool conn_range(const Ctx& c, const FilterOut& fo, uint t, uint& begin, uint& en
   if (k + 1 >= nOffsets) return false;  // the reference reads past the offsets here
   begin = fo.offsets[k];
   end = fo.offsets[k + 1];
-  if (hitEventNumber != c.h.evt[fo.h1[begin]]) return false;
+  // an empty range has no follower whose event the reference could compare
+  // (it reads one past its triplets there); returning gives the same links
+  // and counts as the empty loop
+  if (begin >= end || hitEventNumber != c.h.evt[fo.h1[begin]]) return false;
   return true;
 }
 

@@ -21,6 +21,10 @@ LIB_DIR = os.path.join(HERE, "lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_NAME = "libtrax_gb300.so"
 LIB_PATH = os.path.join(LIB_DIR, LIB_NAME)
+# the bounds-checked debug build (-DTRAX_BOUNDS_CHECK): every data-dependent
+# hit index checked on the device, a bad one failing the call
+CHECKED_OBJ_DIR = os.path.join(LIB_DIR, "obj_checked")
+CHECKED_LIB_PATH = os.path.join(LIB_DIR, "libtrax_gb300_checked.so")
 
 SOURCES = ["k_scan.cu", "k_grid.cu", "k_pairs.cu", "k_triplets.cu", "k_link.cu", "capi.cu", "tune.cu", "k_fit.cu", "host_events.cpp", "k_events.cu", "k_tracks.cu", "k_math.cu"]
 HEADERS = ["trax_device.cuh", "trax_kernels.h", "trax_math.h", "trax_math_coeffs.h", "trax_stages.cuh",
@@ -48,8 +52,8 @@ def _deps_mtime() -> float:
     return max(os.path.getmtime(p) for p in paths)
 
 
-def _compile(src: str, extra) -> str:
-    obj = os.path.join(OBJ_DIR, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, extra, obj_dir: str = OBJ_DIR) -> str:
+    obj = os.path.join(obj_dir, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc()] + NVCC_FLAGS + list(extra) + ["-c", os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -57,22 +61,25 @@ def _compile(src: str, extra) -> str:
     return obj
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> str:
-    """Compile all kernels and the C ABI into trax_gb300/lib/libtrax_gb300.so."""
-    os.makedirs(OBJ_DIR, exist_ok=True)
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= _deps_mtime():
-        return LIB_PATH
-    extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+def build(force: bool = False, verbose_ptxas: bool = False, checked: bool = False) -> str:
+    """Compile all kernels and the C ABI into trax_gb300/lib/libtrax_gb300.so
+    (checked: the bounds-checked debug build, libtrax_gb300_checked.so)."""
+    obj_dir = CHECKED_OBJ_DIR if checked else OBJ_DIR
+    lib_path = CHECKED_LIB_PATH if checked else LIB_PATH
+    os.makedirs(obj_dir, exist_ok=True)
+    if not force and os.path.exists(lib_path) and os.path.getmtime(lib_path) >= _deps_mtime():
+        return lib_path
+    extra = (["-Xptxas", "-v"] if verbose_ptxas else []) + (["-DTRAX_BOUNDS_CHECK"] if checked else [])
     with cf.ThreadPoolExecutor(max_workers=min(len(SOURCES), os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    tmp = LIB_PATH + f".tmp{os.getpid()}"
+        objs = list(ex.map(lambda s: _compile(s, extra, obj_dir), SOURCES))
+    tmp = lib_path + f".tmp{os.getpid()}"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose_ptxas="--ptxas" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose_ptxas="--ptxas" in sys.argv, checked="--checked" in sys.argv))

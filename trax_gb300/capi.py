@@ -91,6 +91,10 @@ _lib = None
 
 
 def library_path() -> str:
+    """The product library, or with TRAX_GB300_BOUNDS_CHECK=1 in the
+    environment its bounds-checked debug build."""
+    if os.environ.get("TRAX_GB300_BOUNDS_CHECK") == "1":
+        return _build.CHECKED_LIB_PATH
     return _build.LIB_PATH
 
 

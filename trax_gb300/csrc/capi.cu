@@ -13,6 +13,7 @@
 //     TRAX_ERR_CAPACITY, never silently truncated.  This mode is captured once
 //     into a CUDA graph and replayed by trax_seed_batch.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -249,6 +250,17 @@ DevHits dev_hits(trax_ctx* c) {
 
 uint32_t* slot(trax_ctx* c, int k) { return ptr<uint32_t>(c->slots) + k; }
 
+// A named NVTX range for the host side of a stage or call (what the
+// reference's per-run cl_event lists and RuntimeRecord classes show,
+// KernelWrapper.hpp:29-33, RuntimeRecord.cpp:123-192); free when no tool
+// is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 // event marks around one kernel (recorded into the graph when capturing)
 // While the stream is being captured the record becomes an event-record node
 // of the graph (cudaEventRecordExternal); otherwise it is a plain record.
@@ -308,6 +320,8 @@ int build_config(trax_ctx* c, bool seeding = true) {
   g.filterThreads = c->filterThreads;
   g.predPairsPerThread = c->predK;
   g.predKeep = c->keepSlots ? c->keepSlots : c->keepAuto;
+  g.nHits = (uint32_t)c->nHits;
+  g.err = slot(c, S_ERR);
   for (uint32_t p = 0; p < g.nLT; ++p) {
     const trax_layer_triplet& t = c->lts[p];
     if (t.layer1 < 1 || t.layer2 < 1 || t.layer3 < 1 || t.layer1 > c->L || t.layer2 > c->L || t.layer3 > c->L)
@@ -398,6 +412,7 @@ int scan_publish(trax_ctx* c, Mode mode, uint32_t* data, uint64_t nHost, const u
 
 // ------------------------------------------------------------------ stages
 int stage_grid(trax_ctx* c, Mode mode) {
+  NvtxRange nvtx("trax.grid");
   const uint64_t n = c->nHits;
   const uint64_t cells = (uint64_t)c->E * c->L * c->cfg.C;
   ENSURE(grid, cells, 4);
@@ -430,6 +445,7 @@ int stage_grid(trax_ctx* c, Mode mode) {
 }
 
 int stage_pairs(trax_ctx* c, Mode mode) {
+  NvtxRange nvtx("trax.pairs");
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   ENSURE(segOuter, S + 1, 4);
   ENSURE(taskBase, S + 1, 4);
@@ -470,6 +486,7 @@ int stage_pairs(trax_ctx* c, Mode mode) {
 }
 
 int stage_predict(trax_ctx* c, Mode mode) {
+  NvtxRange nvtx("trax.predict");
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   const uint32_t* nPairsDev = slot(c, S_PAIRS);
   const uint64_t maxPairs = mode == SYNCED ? c->nPairs : c->capPairs;
@@ -507,6 +524,7 @@ int stage_predict(trax_ctx* c, Mode mode) {
 }
 
 int stage_filter(trax_ctx* c, Mode mode) {
+  NvtxRange nvtx("trax.filter");
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   const uint32_t* nCandsDev = slot(c, S_CANDS);
   const uint64_t maxCands = mode == SYNCED ? c->nCands : c->capCands;
@@ -551,6 +569,7 @@ TripletView triplets(trax_ctx* c, uint64_t maxT) {
 }
 
 int stage_connectivity(trax_ctx* c, Mode mode) {
+  NvtxRange nvtx("trax.connectivity");
   const uint32_t S = c->cfg.E * c->cfg.nLT;
   const uint64_t maxT = mode == SYNCED ? c->nT : c->capT;
   const uint32_t* nTDev = slot(c, S_TRIPLETS);
@@ -619,6 +638,7 @@ int stage_connectivity(trax_ctx* c, Mode mode) {
 }
 
 int stage_fit(trax_ctx* c, Mode mode) {
+  NvtxRange nvtx("trax.circle_fit");
   const uint64_t maxT = mode == SYNCED ? c->nT : c->capT;
   ENSURE(pt, maxT, 4);
   CK(cudaMemsetAsync(c->pt.p, 0, (size_t)std::max<uint64_t>(maxT, 1) * 4, c->st));
@@ -642,6 +662,7 @@ CABuffers ca_buffers(trax_ctx* c) {
 }
 
 int stage_ca(trax_ctx* c, Mode mode) {
+  NvtxRange nvtx("trax.ca");
   if (mode == SYNCED && c->noLinks) {
     c->nTracks = 0;
     return TRAX_OK;
@@ -1451,6 +1472,7 @@ int trax_debug_skip_publish(trax_ctx* c, uint32_t tile) {
 
 int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* stats) {
   if (!c) return TRAX_ERR_ARG;
+  NvtxRange nvtx("trax_seed_batch");
   const bool linking = opts ? opts->run_linking != 0 : true;
   const bool useGraph = opts ? opts->use_graph != 0 : false;
   if (opts && opts->d_eta_cut > 0.0f) c->dEtaCut = opts->d_eta_cut;
@@ -1474,6 +1496,7 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
     const uint64_t key = shape_key(c, linking);
     if (!c->graphExec || key != c->graphKey) {
       // calibrate the capacities with one host-synced run, then capture
+      NvtxRange nvtxCal("trax.calibrate_and_capture");
       ++c->graphCaptures;
       drop_graph(c);
       RC(run_synced_chain(c, linking));
@@ -1498,6 +1521,7 @@ int trax_seed_batch(trax_ctx* c, const trax_batch_opts* opts, trax_batch_stats* 
       c->graphLaunches = c->launches;
       c->graphKey = shape_key(c, linking);
     }
+    NvtxRange nvtxReplay("trax.replay");
     CK(cudaEventRecord(c->ev0, c->st));
     CK(cudaGraphLaunch(c->graphExec, c->st));
     CK(cudaEventRecord(c->ev1, c->st));

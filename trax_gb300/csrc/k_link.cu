@@ -46,7 +46,7 @@ __global__ void eta_kernel(DevConfig cfg, const float4* __restrict__ hits, const
                            const uint32_t* __restrict__ h3, const uint32_t* nTDev, float* eta, uint32_t* seg) {
   const uint32_t nT = *nTDev;
   GRID_STRIDE(t, nT) {
-    const uint32_t hi = h1[t], ho = h3[t];
+    const uint32_t hi = trax_hit(h1[t], cfg), ho = trax_hit(h3[t], cfg);
     const float4 a = hits[hi], b = hits[ho];
     const float px = b.x - a.x, py = b.y - a.y, pz = b.z - a.z;
     const float tt = div_(pz, sqrt_(px * px + py * py));
@@ -107,13 +107,15 @@ __global__ void __launch_bounds__(256)
     uint32_t begin = 0, end = 0, k = 0;
     const uint32_t inner = h2[t], outer = h3[t];
     if (ok) {
-      const uint32_t ev = hitEvt[inner];
-      k = ev * cfg.nLT + (hitLayer[inner] - 1);
+      const uint32_t ev = hitEvt[trax_hit(inner, cfg)];
+      k = ev * cfg.nLT + (hitLayer[trax_hit(inner, cfg)] - 1);
       ok = k < S;  // the reference would read past the offsets
       if (ok) {
         begin = offsets[k];
         end = offsets[k + 1];
-        ok = ev == hitEvt[h1[begin]];  // :130-132
+        // :130-132; an empty range has no follower to compare (the reference
+        // reads one past its triplets there) and gives no links either way
+        ok = begin < end && ev == hitEvt[trax_hit(h1[begin], cfg)];
       }
     }
     if (ok) {

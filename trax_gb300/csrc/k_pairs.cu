@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
     if (!EMIT) {
       s = find_segment(taskBase, S, k);
       i = segOuter[s] + (k - taskBase[s]);
-      const float4 ho = hits[i];
+      const float4 ho = hits[trax_hit(i, cfg)];
       w = pair_window(cfg, s % cfg.nLT, ho.x, ho.y, ho.z, ho.w);
     } else {
       // the count pass's window, segment and ordering of this task
@@ -243,8 +243,8 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
         uint32_t a1, b1, a2, b2;
         pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
         if (simple) simple = rows_in_order(a1, b1, a2, b2, prevEnd);
-        for (uint32_t j = a1; j < b1; ++j) nFound += pair_count_ok(w, hits[j]);
-        for (uint32_t j = a2; j < b2; ++j) nFound += pair_count_ok(w, hits[j]);
+        for (uint32_t j = a1; j < b1; ++j) nFound += pair_count_ok(w, hits[trax_hit(j, cfg)]);
+        for (uint32_t j = a2; j < b2; ++j) nFound += pair_count_ok(w, hits[trax_hit(j, cfg)]);
       }
       taskCount[k] = nFound;
       state.bounds[k] = make_float4(w.zLow, w.zHigh, w.phiLow, w.phiHigh);
@@ -272,12 +272,12 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
             lo0 = a2; hi0 = b2; lo1 = a1; hi1 = b1;
           }
           for (uint32_t j = lo0; j < hi0; ++j)
-            if (pair_ok(t, __ldg(zphi + 2 * (size_t)j))) {
+            if (pair_ok(t, __ldg(zphi + 2 * (size_t)trax_hit(j, cfg)))) {
               if (written < limit) out[written] = make_uint2(j, i);
               ++written;
             }
           for (uint32_t j = lo1; j < hi1; ++j)
-            if (pair_ok(t, __ldg(zphi + 2 * (size_t)j))) {
+            if (pair_ok(t, __ldg(zphi + 2 * (size_t)trax_hit(j, cfg)))) {
               if (written < limit) out[written] = make_uint2(j, i);
               ++written;
             }
@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS)
             pair_row_parts(w, lG1, C, nP, zs, a1, b1, a2, b2);
             visited = (a1 <= j && j < b1) || (a2 <= j && j < b2);
           }
-          if (visited && pair_valid(w, hits[j])) out[written++] = make_uint2(j, i);
+          if (visited && pair_valid(w, hits[trax_hit(j, cfg)])) out[written++] = make_uint2(j, i);
         }
       }
       if (written < limit) {

@@ -54,11 +54,12 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
     const uint2 pr = gid < nPairs ? pairs[gid] : make_uint2(TRAX_SENTINEL, TRAX_SENTINEL);
     uint32_t count = 0;
     if (pr.x != TRAX_SENTINEL) {
-      const uint32_t event = hitEvt[pr.x];
-      const uint32_t lt = hitLayer[pr.x] - 1;  // Q7
+      const uint32_t hx = trax_hit(pr.x, cfg), hy = trax_hit(pr.y, cfg);
+      const uint32_t event = hitEvt[hx];
+      const uint32_t lt = hitLayer[hx] - 1;  // Q7
       const uint32_t layer = cfg.layer3[lt] - 1;
       const uint32_t* lG3 = grid + ((size_t)event * cfg.L + layer) * cfg.C;
-      const PredUnionWindow w = pred_union_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
+      const PredUnionWindow w = pred_union_window(cfg, lt, layer, hits[hx], hits[hy]);
       // One walk over the union of both variants' z rows with each
       // variant's own z test (pred_union_window: a hit outside a variant's
       // rows fails its test); the phi test is common.  Each variant's valid
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
         for (int part = 0; part < 2; ++part) {
 #pragma unroll 2
           for (uint32_t j = a[part]; j < b[part]; ++j) {
-            const float2 h = __ldg(zphi + 2 * (size_t)j);
+            const float2 h = __ldg(zphi + 2 * (size_t)trax_hit(j, cfg));
             const bool lo = w.phiLow <= h.y, hi = h.y <= w.phiHigh;
             const bool phiOk = wrap ? (lo || hi) : (lo && hi);
             count += (phiOk && zl0 <= h.x && h.x <= zh0);
@@ -164,10 +165,11 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
       const uint2 pr = gid < nPairs ? pairs[gid] : make_uint2(TRAX_SENTINEL, TRAX_SENTINEL);
       PredStage& ps = st[32 * k];
       if (pr.x != TRAX_SENTINEL) {
-        const uint32_t event = hitEvt[pr.x];
-        const uint32_t lt = hitLayer[pr.x] - 1;  // Q7
+        const uint32_t hx = trax_hit(pr.x, cfg), hy = trax_hit(pr.y, cfg);
+        const uint32_t event = hitEvt[hx];
+        const uint32_t lt = hitLayer[hx] - 1;  // Q7
         const uint32_t layer = cfg.layer3[lt] - 1;
-        const PredWindow w = pred_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
+        const PredWindow w = pred_window(cfg, lt, layer, hits[hx], hits[hy]);
         ps.zLow[0] = w.zLow[0];
         ps.zHigh[0] = w.zHigh[0];
         ps.zLow[1] = w.zLow[1];
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
     bool live = advance();
     while (__any_sync(0xffffffffu, live)) {
       if (live) {
-        const float2 h = __ldg(zphi + 2 * (size_t)j);
+        const float2 h = __ldg(zphi + 2 * (size_t)trax_hit(j, cfg));
         const bool phiOk = (pa1 <= h.y && h.y <= pb1) || (pa2 <= h.y && h.y <= pb2);
         cnt += (phiOk && zl0 <= h.x && h.x <= zh0);
         if (phiOk && zl1 <= h.x && h.x <= zh1) {
@@ -338,11 +340,12 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
       continue;
     }
     const uint2 pr = pairs[gid];
-    const uint32_t event = hitEvt[pr.x];
-    const uint32_t lt = hitLayer[pr.x] - 1;
+    const uint32_t hx = trax_hit(pr.x, cfg), hy = trax_hit(pr.y, cfg);
+    const uint32_t event = hitEvt[hx];
+    const uint32_t lt = hitLayer[hx] - 1;
     const uint32_t layer = cfg.layer3[lt] - 1;
     const uint32_t* lG3 = grid + ((size_t)event * cfg.L + layer) * cfg.C;
-    const PredWindow w = pred_store_window(cfg, lt, layer, hits[pr.x], hits[pr.y]);
+    const PredWindow w = pred_store_window(cfg, lt, layer, hits[hx], hits[hy]);
     uint32_t n = 0;
     const uint32_t C = cfg.C, nP = cfg.nP;
     for (uint32_t zs = w.zLoSec[1]; zs < w.zHiSec[1] && n < limit; ++zs) {
@@ -350,7 +353,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
       pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
       for (int part = 0; part < 2 && n < limit; ++part)
         for (uint32_t j = a[part]; j < b[part] && n < limit; ++j)
-          if (pred_valid(w, 1, hits[j])) out[n++] = make_uint2(gid, j);
+          if (pred_valid(w, 1, hits[trax_hit(j, cfg)])) out[n++] = make_uint2(gid, j);
     }
     sent += limit - n;
     for (; n < limit; ++n) out[n] = make_uint2(gid, TRAX_SENTINEL);
@@ -411,7 +414,8 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
   auto rest = [&](uint32_t g0, uint32_t g) {
     const uint2 c = cands[g];
     const uint2 pr = pairs[c.x];
-    if (filter_rest(cfg, hitLayer[pr.x] - 1, hits[pr.x], hits[pr.y], hits[c.y]))
+    const uint32_t hx = trax_hit(pr.x, cfg);
+    if (filter_rest(cfg, hitLayer[hx] - 1, hits[hx], hits[trax_hit(pr.y, cfg)], hits[trax_hit(c.y, cfg)]))
       atomicOr(&bits[(g - g0) >> 5], 1u << (g & 31u));
   };
   for (uint32_t g0 = (blockIdx.x * (blockDim.x >> 5) + warp) * (WORDS * 32); g0 < n; g0 += warps * WORDS * 32) {
@@ -425,7 +429,9 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
         const uint2 c = cands[g];
         if (c.y != TRAX_SENTINEL) {  // a slot the reference never wrote fails
           const uint2 pr = pairs[c.x];
-          pass = filter_dphi_fast(cfg, hitLayer[pr.x] - 1, hits[pr.x], hits[pr.y], hits[c.y]);
+          const uint32_t hx = trax_hit(pr.x, cfg);
+          pass = filter_dphi_fast(cfg, hitLayer[hx] - 1, hits[hx], hits[trax_hit(pr.y, cfg)],
+                                  hits[trax_hit(c.y, cfg)]);
         }
       }
       const uint32_t ballot = __ballot_sync(0xffffffffu, pass);
@@ -514,7 +520,7 @@ __global__ void triplet_offsets_kernel(DevConfig cfg, const uint32_t* __restrict
                                        const uint32_t* nTDev, uint32_t* offsets) {
   const uint32_t nT = *nTDev;
   for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < nT; gid += gridDim.x * blockDim.x) {
-    const uint32_t hitId = h1[gid];
+    const uint32_t hitId = trax_hit(h1[gid], cfg);
     const uint32_t layerTriplet = hitLayer[hitId];
     const uint32_t event = hitEvt[hitId];
     if (gid > 0) {

@@ -39,6 +39,8 @@ struct DevConfig {
   uint32_t pairThreads, predThreads, filterThreads;
   uint32_t predPairsPerThread;  // 1, 2 or 4 pairs per thread in the prediction count pass
   uint32_t predKeep;            // candidates captured per pair by the count pass (4, 8, 16 or 32)
+  uint32_t nHits;               // hits of the batch (the length of every per-hit array)
+  uint32_t* err;                // the context's device error word
 };
 
 #define TRAX_MAX_TUNED_THREADS 256
@@ -58,6 +60,22 @@ struct DevHits {
 
 __device__ __forceinline__ void raise_error(uint32_t* err, uint32_t bit) {
   if (err) atomicOr(err, bit);
+}
+
+// A hit index that comes from data (grid offsets, pairs, candidates,
+// triplets).  Bounds-checked builds (-DTRAX_BOUNDS_CHECK) record
+// TRAX_EBIT_BOUNDS in the context's error word for an index outside the
+// batch and read hit 0 instead, so that the call fails with
+// TRAX_ERR_DEVICE_ASSERT and no access leaves the arrays; other builds use
+// the index as it is.  A debugging aid where no memory checker runs.
+__device__ __forceinline__ uint32_t trax_hit(uint32_t i, const DevConfig& cfg) {
+#if defined(TRAX_BOUNDS_CHECK)
+  if (i >= cfg.nHits) {
+    raise_error(cfg.err, TRAX_EBIT_BOUNDS);
+    return 0u;
+  }
+#endif
+  return i;
 }
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
