@@ -65,6 +65,9 @@ def lib():
             L.ref_copy.restype = ctypes.c_int
             L.ref_free.argtypes = [ctypes.c_void_p]
             L.ref_prefix_sum.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32]
+            L.ref_track_metrics.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_uint64] + \
+                [ctypes.c_void_p] * 5
+            L.ref_track_metrics.restype = None
             L.ref_ca.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
                                  ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_void_p)]
             L.ref_ca.restype = ctypes.c_int
@@ -136,6 +139,20 @@ def run_events(batch, workers: int, n_threads: int = 1, local_mem: int = CPU_LOC
     if L.ref_run_events(ctypes.byref(inp), n_threads, local_mem, workers, out.ctypes.data) != 0:
         raise RuntimeError(L.ref_last_error().decode())
     return out
+
+
+def track_metrics(tracks, track_offsets, h1, h2, h3, hit_track_id) -> dict:
+    """The reference's own track evaluation (TripletBuilder.cpp: extractTracks,
+    cloneRemoval, splitRealFakeTracks, findUniqueRealTracks) on a CA output:
+    the counts printTracks reports."""
+    L = lib()
+    cols = [np.ascontiguousarray(a, dtype=np.uint32) for a in (tracks, track_offsets, h1, h2, h3, hit_track_id)]
+    cols = [c if c.size else np.zeros(1, np.uint32) for c in cols]
+    out = np.zeros(5, np.uint64)
+    n_entries, n_offsets = np.asarray(tracks).size, np.asarray(track_offsets).size
+    L.ref_track_metrics(cols[0].ctypes.data, n_entries, cols[1].ctypes.data, n_offsets, cols[2].ctypes.data,
+                        cols[3].ctypes.data, cols[4].ctypes.data, cols[5].ctypes.data, out.ctypes.data)
+    return dict(zip(("total", "filtered", "valid", "valid_unique", "fakes"), (int(v) for v in out)))
 
 
 def prefix_sum(data: np.ndarray, wg: int) -> np.ndarray:

@@ -50,6 +50,7 @@
 #include <vector>
 
 #include "ref_kernels.cpp"
+#include "ref_tracks.cpp"
 #include "trax_oracle.h"
 
 namespace refrt {
@@ -892,6 +893,39 @@ void ref_prefix_sum(uint32_t* data, uint32_t n, uint32_t wg) {
   Buf<uint> b = upload(data, n, kUninit);
   PrefixSum().run(b.p(), n, wg);
   memcpy(data, b.p(), (size_t)n * 4);
+}
+
+// The reference's track evaluation on a CA output: its extractTracks,
+// cloneRemoval, splitRealFakeTracks and findUniqueRealTracks
+// (TripletBuilder.cpp, in ref_tracks.cpp), and the five counts printTracks
+// reports from them (TripletBuilder.cpp:1016-1021, 1047-1051): out5 = total, filtered,
+// valid, valid unique, fakes.  tracks[n_entries] and track_offsets
+// [n_offsets] are the CA's trackCollection and its handler prefix sum;
+// h1..h3 the triplets; hit_id the simulated track of every hit.
+void ref_track_metrics(const uint32_t* tracks, uint64_t n_entries, const uint32_t* track_offsets,
+                       uint64_t n_offsets, const uint32_t* h1, const uint32_t* h2, const uint32_t* h3,
+                       const uint32_t* hit_id, uint64_t* out5) {
+  using namespace reftr;
+  const std::vector<uint> vTrackCollection(tracks, tracks + n_entries);
+  const std::vector<uint> vPSum(track_offsets, track_offsets + n_offsets);
+  const std::vector<float> vPt;  // unused by extractTracks
+  TrackletCollection tracklets;
+  tracklets.h1 = h1;
+  tracklets.h2 = h2;
+  tracklets.h3 = h3;
+  HitCollection hits;
+  hits.hitId = hit_id;
+  TrackCollection reconstructed;
+  if (n_offsets > 0) reconstructed = extractTracks(vTrackCollection, vPSum, &tracklets, hits, vPt);
+  const TrackCollection filtered = cloneRemoval(reconstructed);
+  TrackCollection real, fake;
+  std::tie(real, fake) = splitRealFakeTracks(filtered, hits);
+  const std::map<uint, Track> unique = findUniqueRealTracks(real, hits);
+  out5[0] = reconstructed.size();
+  out5[1] = filtered.size();
+  out5[2] = real.size();
+  out5[3] = unique.size();
+  out5[4] = fake.size();
 }
 
 }  // extern "C"

@@ -10,7 +10,11 @@ runtime.  Its kernels, though, are OpenCL C source text inside
    ``/root/reference``) and copies the text of every kernel on the seeding
    path into ``oracle/_ref/ref_kernels.cpp``, inside ``namespace refk``,
    after ``oracle/ref_shim.h`` (the OpenCL work-item environment);
-2. compiles it with ``oracle/ref_driver.cpp`` (the reference's host-side
+2. copies the track evaluation of ``src/triplet_builder/TripletBuilder.cpp``
+   (track extraction, clone removal, real/fake split; host C++ over std
+   containers) into ``oracle/_ref/ref_tracks.cpp``, inside ``namespace
+   reftr``, with comments removed and nothing else changed;
+3. compiles both with ``oracle/ref_driver.cpp`` (the reference's host-side
    ``run()`` sequences, restated) into ``oracle/_ref/libtraxref.so``.
 
 Nothing it writes is committed: ``oracle/_ref/`` is git-ignored.  When the
@@ -42,6 +46,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 OUT_DIR = os.path.join(HERE, "_ref")
 GEN_CPP = os.path.join(OUT_DIR, "ref_kernels.cpp")
+GEN_TRACKS = os.path.join(OUT_DIR, "ref_tracks.cpp")
+# the reference's track evaluation (host C++ over std containers): track
+# extraction from the CA output, clone removal, real/fake split, distinct
+# real tracks; copied from the Track typedef up to printTracks
+TRACKS_SRC = "src/triplet_builder/TripletBuilder.cpp"
+TRACKS_FIRST = "typedef typename std::pair<uint, std::shared_ptr<std::vector<uint>>> Track;"
+TRACKS_END = "void printTracks("
 LIB_PATH = os.path.join(OUT_DIR, "libtraxref.so")
 DRIVER = os.path.join(HERE, "ref_driver.cpp")
 SHIM = os.path.join(HERE, "ref_shim.h")
@@ -177,6 +188,36 @@ def generate(root: str) -> Dict[str, bool]:
     return barriers
 
 
+def generate_tracks(root: str) -> None:
+    """Writes oracle/_ref/ref_tracks.cpp: TripletBuilder.cpp's track evaluation
+    functions, verbatim but for the comments, inside namespace reftr, where
+    ref_shim.h gives them the HitCollection / TrackletCollection accessors
+    they call."""
+    raw = open(os.path.join(root, TRACKS_SRC), encoding="utf-8", errors="replace").read().splitlines()
+    first = next(i for i, ln in enumerate(raw) if ln.strip() == TRACKS_FIRST)
+    last = next(i for i, ln in enumerate(raw) if i > first and ln.startswith(TRACKS_END))
+    body = strip_comments("\n".join(raw[first:last]))
+    lines = [
+        "// GENERATED by oracle/ref_extract.py -- the reference's track evaluation,",
+        "// copied from " + TRACKS_SRC + " (comments removed).  Not committed;",
+        "// rebuilt by the recipe.",
+        '#include "ref_shim.h"',
+        "",
+        "namespace reftr {",
+        "using std::shared_ptr;  // the reference's own headers bring it in",
+        "",
+        f"// {TRACKS_SRC}:{first + 1}-{last}",
+        body,
+        "",
+        "}  // namespace reftr",
+        "",
+    ]
+    tmp = GEN_TRACKS + f".tmp{os.getpid()}"
+    with open(tmp, "w") as f:
+        f.write("\n".join(lines))
+    os.replace(tmp, GEN_TRACKS)
+
+
 CXXFLAGS = ["-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
             "-Wall", "-Wno-int-in-bool-context", "-Wno-unused-variable", "-Wno-unused-but-set-variable", "-Wno-sign-compare",
             "-Wfloat-conversion", "-Werror=narrowing"]
@@ -213,15 +254,17 @@ def build(force: bool = False) -> str:
     root = reference_dir()
     have_ref = os.path.isdir(os.path.join(root, "src", "algorithms"))
     if have_ref:
-        srcs = [os.path.join(root, h) for h, _ in KERNELS] + [os.path.join(root, PREFIX_DEFINES_SRC)]
-        stale = (force or not os.path.exists(GEN_CPP)
-                 or os.path.getmtime(GEN_CPP) < max([os.path.getmtime(s) for s in srcs] + [_newest_input()]))
-        if stale:
+        srcs = [os.path.join(root, h) for h, _ in KERNELS] + [os.path.join(root, PREFIX_DEFINES_SRC),
+                                                              os.path.join(root, TRACKS_SRC)]
+        newest = max([os.path.getmtime(s) for s in srcs] + [_newest_input()])
+        if force or not os.path.exists(GEN_CPP) or os.path.getmtime(GEN_CPP) < newest:
             generate(root)
-    elif not os.path.exists(GEN_CPP):
+        if force or not os.path.exists(GEN_TRACKS) or os.path.getmtime(GEN_TRACKS) < newest:
+            generate_tracks(root)
+    elif not (os.path.exists(GEN_CPP) and os.path.exists(GEN_TRACKS)):
         return ""
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
-            os.path.getmtime(GEN_CPP), _newest_input()):
+            os.path.getmtime(GEN_CPP), os.path.getmtime(GEN_TRACKS), _newest_input()):
         compile_lib()
     return LIB_PATH
 

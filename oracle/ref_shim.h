@@ -197,3 +197,47 @@ inline V atomic_max(volatile V* p, A v) {
 }
 
 }  // namespace refk
+
+// ---------------------------------------------------------------------------
+// The accessors the reference's track evaluation (TripletBuilder.cpp, copied
+// into ref_tracks.cpp) calls: HitCollection::getValue(HitId/GlobalX/Y/Z(), i)
+// (HitCollection.h:23-62) and TrackletCollection::getValue(TrackletHit1/2/3(),
+// t) (TrackletCollection.h:32-78), over plain arrays.
+#include <algorithm>
+#include <iostream>
+#include <list>
+#include <map>
+#include <memory>
+#include <utility>
+#include <vector>
+
+namespace reftr {
+typedef unsigned int uint;
+struct HitId {};
+struct GlobalX {};
+struct GlobalY {};
+struct GlobalZ {};
+struct TrackletHit1 {};
+struct TrackletHit2 {};
+struct TrackletHit3 {};
+
+struct HitCollection {
+  const uint32_t* hitId = nullptr;  // simulated track of each hit
+  const float* x = nullptr;         // coordinates (printTrack only; may be null)
+  const float* y = nullptr;
+  const float* z = nullptr;
+  uint getValue(HitId, uint i) const { return hitId[i]; }
+  float getValue(GlobalX, uint i) const { return x ? x[i] : 0.0f; }
+  float getValue(GlobalY, uint i) const { return y ? y[i] : 0.0f; }
+  float getValue(GlobalZ, uint i) const { return z ? z[i] : 0.0f; }
+};
+
+struct TrackletCollection {
+  const uint32_t* h1 = nullptr;
+  const uint32_t* h2 = nullptr;
+  const uint32_t* h3 = nullptr;
+  uint getValue(TrackletHit1, uint t) const { return h1[t]; }
+  uint getValue(TrackletHit2, uint t) const { return h2[t]; }
+  uint getValue(TrackletHit3, uint t) const { return h3[t]; }
+};
+}  // namespace reftr
