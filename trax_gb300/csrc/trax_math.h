@@ -166,7 +166,7 @@ TRAX_HD float cl_max(float x, float y) { return (x < y) ? y : x; }
 template <int N>
 TRAX_HD float horner(const float (&c)[N], float u) {
   float p = c[N - 1];
-#if defined(__CUDACC__)
+#if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
   for (int k = N - 2; k >= 0; --k) {
