@@ -405,18 +405,60 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
                   uint32_t* masks, uint32_t* warpSums, uint32_t* nWordsOut) {
   constexpr uint32_t WORDS = 32;  // a warp takes 32 words = 1024 candidates at a time
   __shared__ uint32_t s_queue[TRAX_MAX_TUNED_THREADS / 32][64];
+  __shared__ uint32_t s_queue2[TRAX_MAX_TUNED_THREADS / 32][64];
   __shared__ uint32_t s_bits[TRAX_MAX_TUNED_THREADS / 32][WORDS];
   const uint32_t n = *nCandsDev;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   uint32_t* queue = s_queue[warp];
+  uint32_t* queue2 = s_queue2[warp];
   uint32_t* bits = s_bits[warp];
-  auto rest = [&](uint32_t g0, uint32_t g) {
+  // The cuts after dphi in the order that rejects most first: the circle
+  // (TIP and curvature) keeps about a third of the dphi survivors (an eighth
+  // in pileup), dtheta nearly all.  The circle's survivors wait in a second
+  // per-warp queue, so that dtheta runs 32 at a time on them only.  The four
+  // cuts are independent tests of the same candidate, ANDed, so their order
+  // changes no outcome.
+  struct Cand {
+    float4 A, B, C;
+    uint32_t lt;
+  };
+  auto load = [&](uint32_t g) {
     const uint2 c = cands[g];
     const uint2 pr = pairs[c.x];
     const uint32_t hx = trax_hit(pr.x, cfg);
-    if (filter_rest(cfg, hitLayer[hx] - 1, hits[hx], hits[trax_hit(pr.y, cfg)], hits[trax_hit(c.y, cfg)]))
-      atomicOr(&bits[(g - g0) >> 5], 1u << (g & 31u));
+    return Cand{hits[hx], hits[trax_hit(pr.y, cfg)], hits[trax_hit(c.y, cfg)], hitLayer[hx] - 1};
+  };
+  uint32_t queued2 = 0;  // warp-uniform
+  // dtheta on the first 32 queued circle survivors (items of lanes < active)
+  auto dtheta_round = [&](uint32_t g0, uint32_t active) {
+    if (lane < active) {
+      const uint32_t g = queue2[lane];
+      const Cand k = load(g);
+      if (filter_dtheta(cfg, k.lt, k.A, k.B, k.C)) atomicOr(&bits[(g - g0) >> 5], 1u << (g & 31u));
+    }
+    __syncwarp();
+  };
+  // the circle on one dphi survivor per lane (lanes < active); survivors
+  // join the second queue, which runs dtheta whenever it holds 32
+  auto circle_round = [&](uint32_t g0, uint32_t active) {
+    bool ok = false;
+    uint32_t g = 0;
+    if (lane < active) {
+      g = queue[lane];
+      const Cand k = load(g);
+      ok = filter_circle(cfg, k.lt, k.A, k.B, k.C);
+    }
+    const uint32_t ballot = __ballot_sync(0xffffffffu, ok);
+    if (ok) queue2[queued2 + __popc(ballot & lanemask_lt())] = g;
+    queued2 += __popc(ballot);
+    __syncwarp();
+    if (queued2 >= 32) {
+      dtheta_round(g0, 32u);
+      if (lane < queued2 - 32) queue2[lane] = queue2[32 + lane];
+      queued2 -= 32;
+      __syncwarp();
+    }
   };
   for (uint32_t g0 = (blockIdx.x * (blockDim.x >> 5) + warp) * (WORDS * 32); g0 < n; g0 += warps * WORDS * 32) {
     bits[lane] = 0u;
@@ -438,16 +480,16 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
       if (pass) queue[queued + __popc(ballot & lanemask_lt())] = g;
       queued += __popc(ballot);
       __syncwarp();
-      if (queued >= 32) {  // a full round of the remaining tests
-        rest(g0, queue[lane]);
-        __syncwarp();
+      if (queued >= 32) {  // a full round of the circle cut
+        circle_round(g0, 32u);
         if (lane < queued - 32) queue[lane] = queue[32 + lane];
         queued -= 32;
         __syncwarp();
       }
     }
-    if (lane < queued) rest(g0, queue[lane]);
-    __syncwarp();
+    circle_round(g0, queued);
+    dtheta_round(g0, queued2);
+    queued2 = 0;
     const uint32_t word = (g0 >> 5) + lane;
     if (g0 + lane * 32 < n) {
       const uint32_t b = bits[lane];

@@ -257,13 +257,17 @@ __device__ __forceinline__ bool filter_dphi_fast(const DevConfig& cfg, uint32_t 
   return q > 0 || (q < 0 && filter_dphi(cfg.dPhiCut[lt], A, B, Cc));
 }
 
-// The dtheta, TIP and curvature parts (:84-117, :130-154).
-__device__ __forceinline__ bool filter_rest(const DevConfig& cfg, uint32_t lt, float4 A, float4 B, float4 Cc) {
-  bool valid = true;
+// The dtheta part (:84-117): the polar angles of the two segments.
+__device__ __forceinline__ bool filter_dtheta(const DevConfig& cfg, uint32_t lt, float4 A, float4 B, float4 Cc) {
   const float theta1 = atan2_(sqrt_((B.x - A.x) * (B.x - A.x) + (B.y - A.y) * (B.y - A.y)), (B.z - A.z));
   const float angle2 = atan2_(sqrt_((Cc.x - B.x) * (Cc.x - B.x) + (Cc.y - B.y) * (Cc.y - B.y)), (Cc.z - B.z));
   const float delta = fabs_(div_(angle2, theta1));
-  valid = valid && (1 - cfg.dThetaCut[lt] <= delta && delta <= 1 + cfg.dThetaCut[lt]);
+  return 1 - cfg.dThetaCut[lt] <= delta && delta <= 1 + cfg.dThetaCut[lt];
+}
+
+// The TIP and curvature parts (:130-154): the circle through the three hits
+// from the paraboloid plane, its point closest to the beam line and radius.
+__device__ __forceinline__ bool filter_circle(const DevConfig& cfg, uint32_t lt, float4 A, float4 B, float4 Cc) {
   const f3 pP1 = make_f3(A.x, A.y, A.x * A.x + A.y * A.y);
   const f3 pP2 = make_f3(B.x, B.y, B.x * B.x + B.y * B.y);
   const f3 pP3 = make_f3(Cc.x, Cc.y, Cc.x * Cc.x + Cc.y * Cc.y);
@@ -280,9 +284,13 @@ __device__ __forceinline__ bool filter_rest(const DevConfig& cfg, uint32_t lt, f
   const float pCAy = cOy + cR * vy;
   const float tip_squared = pCAx * pCAx + pCAy * pCAy;
   const float tipCut = cfg.tipCut[lt];
-  valid = valid && (tip_squared <= (tipCut * tipCut));
-  valid = valid && (cR >= cfg.minRcurv);
-  return valid;
+  return tip_squared <= (tipCut * tipCut) && cR >= cfg.minRcurv;
+}
+
+// The dtheta, TIP and curvature parts together.
+__device__ __forceinline__ bool filter_rest(const DevConfig& cfg, uint32_t lt, float4 A, float4 B, float4 Cc) {
+  const bool dtheta = filter_dtheta(cfg, lt, A, B, Cc);
+  return filter_circle(cfg, lt, A, B, Cc) && dtheta;
 }
 
 }  // namespace trax
