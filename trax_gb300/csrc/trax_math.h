@@ -8,7 +8,9 @@
 // round-to-nearest operations.  Vendor libraries (glibc libm, CUDA's libdevice)
 // differ from each other in the last bits, so this header provides its own
 // implementations built only from + - * / sqrt, comparisons and integer bit
-// manipulation, evaluated without fused multiply-add:
+// manipulation, evaluated without contraction, and the polynomial steps as
+// explicit fused multiply-adds (fmaf: one rounding, IEEE-754's fusedMultiplyAdd,
+// so the same bits on the CPU and the GPU):
 //   * nvcc: -fmad=false -prec-div=true -prec-sqrt=true -ftz=false
 //   * g++ : -ffp-contract=off (and no -ffast-math)
 //
@@ -162,17 +164,14 @@ TRAX_HD float cl_sign(float x) {
 TRAX_HD float cl_max(float x, float y) { return (x < y) ? y : x; }
 
 // ------------------------------------------------------ polynomial kernels
-// P(u) by Horner, one rounding per operation.
+// P(u) by Horner, one rounding per step: p = fma(p, u, c[k]).
 template <int N>
 TRAX_HD float horner(const float (&c)[N], float u) {
   float p = c[N - 1];
 #if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
-  for (int k = N - 2; k >= 0; --k) {
-    p = p * u;
-    p = p + c[k];
-  }
+  for (int k = N - 2; k >= 0; --k) p = fmaf(p, u, c[k]);
   return p;
 }
 
