@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
         pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
 #pragma unroll
         for (int part = 0; part < 2; ++part) {
-#pragma unroll 2
+#pragma unroll 4
           for (uint32_t j = a[part]; j < b[part]; ++j) {
             const float2 h = __ldg(zphi + 2 * (size_t)trax_hit(j, cfg));
             const bool lo = w.phiLow <= h.y, hi = h.y <= w.phiHigh;
