@@ -75,6 +75,9 @@ def parse():
     p.add_argument("--no-align", action="store_true", help="skip the alignment (differentiable fit) measurement")
     p.add_argument("--no-config3", action="store_true", help="skip the high-occupancy (config 3) measurement")
     p.add_argument("--config3-steps", type=int, default=10)
+    p.add_argument("--config3-events", type=int, default=16, help="events of the config 3 batch (16: the full workload)")
+    p.add_argument("--config3-fine", type=int, default=8,
+                   help="fine z rows per grid row of config 3's prediction count (0: none)")
     p.add_argument("--runtime-csv", default=None, help="write the timed steps as the reference's runtime csv")
     p.add_argument("--grid", default=None, help="z x phi sectors, e.g. 200x256 (default: autotuned)")
     p.add_argument("--no-tune", action="store_true", help="skip the autotuner (grid of the workload, default blocks)")
@@ -431,15 +434,18 @@ def run_alignment(device: int):
         ctx.close()
 
 
-def run_config3(device: int, steps: int):
+def run_config3(device: int, steps: int, n_events: int = 16, fine: int = 8):
     """The high-occupancy workload at full size (16 events x 20 vertices x 1000
     tracks, about 125 000 hits per event, grid 80 x 256): one CUDA-graph replay
-    of the whole chain per step, device time from CUDA events."""
+    of the whole chain per step, device time from CUDA events.  The prediction
+    count walks a z grid `fine` times finer than the grid's 7.5 cm rows (the
+    same results; 0: the grid itself)."""
     from trax_gb300 import capi, events
-    batch = events.generate(3)
+    batch = events.generate(3, n_events=n_events)
     ctx = capi.Context(device)
     try:
         ctx.upload(batch)
+        ctx.set_fine_rows(fine)
         first = ctx.seed_batch(use_graph=True)  # calibrates the capacities and captures the graph
         for _ in range(2):
             ctx.seed_batch(use_graph=True)
@@ -449,8 +455,8 @@ def run_config3(device: int, steps: int):
             ms.append(st.device_ms)
             captures += st.graph_captures
         t = float(np.mean(ms))
-        return {"workload": "pileup: 16 events x 20 vertices x 1000 tracks + 5% noise, 10 layers, 6 layer triplets, "
-                            "grid 80x256, seed 3 (config 3)",
+        return {"workload": f"pileup: {batch.n_events} events x 20 vertices x 1000 tracks + 5% noise, 10 layers, "
+                            "6 layer triplets, grid 80x256, seed 3 (config 3)",
                 "events_per_s": round(batch.n_events / (t * 1e-3), 2), "ms_per_batch": round(t, 3),
                 "steps": len(ms), "hits": batch.n_hits,
                 "sizes": {"pairs": st.n_pairs, "candidates": st.n_candidates, "triplets": st.n_triplets,
@@ -463,6 +469,7 @@ def run_config3(device: int, steps: int):
                                            "a capacity overflow"},
                 "kernel_launches_per_step": st.kernel_launches,
                 "candidate_slots": ctx.candidate_slots(),
+                "fine_rows": ctx.fine_rows(),
                 "kernel_ms": {k: round(v, 3) for k, v in ctx.timings()[1].items() if v >= 0},
                 "parity": "tests/test_gpu_parity.py::test_pileup_workload_at_full_size: every array equals the "
                           "oracle run on the whole batch"}
@@ -553,6 +560,7 @@ def run_ours(args, ranks):
                    "block_sizes": {k: shape[k] for k in ("pair_threads", "predict_threads", "filter_threads")},
                    "predict_pairs_per_thread": ctx.pairs_per_thread(),
                    "predict_candidate_slots": ctx.candidate_slots(),
+                   "predict_fine_rows": ctx.fine_rows(),
                    "autotune": None if tune is None else {
                        "shapes_timed": tune["shapes_timed"], "from_cache": bool(tune["from_cache"]),
                        "best_ms": round(tune["best_ms"], 4), "default_shape_ms": round(tune["default_ms"], 4)},
@@ -633,6 +641,7 @@ def run_ours(args, ranks):
                                shape_now["filter_threads"])
             c2.set_pairs_per_thread(ctx.pairs_per_thread())
             c2.set_candidate_slots(tune["candidate_slots"] if tune else 0)
+            c2.set_fine_rows(ctx.fine_rows())
             for _w in range(2):
                 c2.seed_batch(use_graph=True)
             outs = ([capi.pinned_empty((max(st.n_triplets, 1),), np.uint32) for _ in range(3)]
@@ -695,7 +704,7 @@ def run_ours(args, ranks):
         if not args.no_align:
             result["alignment"] = run_alignment(device)
         if not args.no_config3:
-            result["config3"] = run_config3(device, args.config3_steps)
+            result["config3"] = run_config3(device, args.config3_steps, args.config3_events, args.config3_fine)
     ctx.close()
     return result
 

@@ -275,6 +275,20 @@ int trax_get_pairs_per_thread(trax_ctx* ctx, uint32_t* k);
  * effect; trax_autotune tunes it after the pairs per thread. */
 int trax_set_candidate_slots(trax_ctx* ctx, uint32_t k);
 int trax_get_candidate_slots(trax_ctx* ctx, uint32_t* k);
+/* Rows of the prediction count's fine z grid per row of the grid: 0 (none,
+ * the default), 2, 4, 8 or 16.  With f > 0 the grid stage also sorts every
+ * layer's grid-ordered hits by a z grid f times finer (f rows inside each
+ * z row, the same phi columns), and the count pass walks only the fine rows
+ * its window reaches; it finds the same hits and captures the same
+ * candidates, so the results do not change.  It pays off where a grid row
+ * is much longer than the windows (many hits walked per pair fail the z
+ * test); it costs a second grid (4 bytes per fine cell per (event, layer))
+ * and its build.  Pairs per thread do not apply to it.  No counterpart in
+ * the reference, whose predictCount walks the grid's rows
+ * (TripletThetaPhiPredictor.h:187-219); trax_autotune tunes it after the
+ * candidate slots. */
+int trax_set_fine_rows(trax_ctx* ctx, uint32_t f);
+int trax_get_fine_rows(trax_ctx* ctx, uint32_t* f);
 
 /* ------------------------------------------------------------- batched
  * The whole chain (buildTriplets, TripletBuilder.cpp:312-467) for all
@@ -287,8 +301,9 @@ int trax_seed_batch(trax_ctx* ctx, const trax_batch_opts* opts, trax_batch_stats
  * (grid.nSectorsZ / grid.nSectorsPhi, TripletBuilder.cpp:631-634) and work-group sizes
  * are fixed.  It times CUDA-graph replays of trax_seed_batch on the uploaded
  * hits for grid sizes n_z x n_phi (cells per layer within the shared-memory
- * grid build) and then for the three kernels' block sizes, one coordinate at
- * a time, and leaves the fastest shape set on the context.  The result is
+ * grid build), then for the three kernels' block sizes, one coordinate at
+ * a time, then for the prediction count's pairs per thread, candidate slots
+ * and fine z grid, and leaves the fastest shape set on the context.  The result is
  * cached in the JSON file `cache_path` (may be NULL: no cache), keyed by a
  * hash of the workload (batch shape, layer triplets, geometry, minimum pT,
  * whether linking runs) and the GPU's SM count; a cached shape is applied
@@ -306,6 +321,8 @@ typedef struct trax_tune_result {
   uint32_t shapes_timed;     /* shapes timed by this call */
   uint32_t pairs_per_thread; /* of the prediction count (trax_set_pairs_per_thread) */
   uint32_t candidate_slots;  /* trax_set_candidate_slots: 0 = the library's choice */
+  uint32_t fine_rows;        /* trax_set_fine_rows */
+  uint32_t reserved;         /* 0 */
   double best_ms;            /* device time of one chain replay at the chosen shape */
   double default_ms;         /* the same for the shape the context had before */
 } trax_tune_result;

@@ -4,7 +4,8 @@ No memory checker runs on this hardware, so this build checks every
 data-dependent hit index on the device (grid offsets, pairs, candidates,
 triplets): an index outside the batch sets TRAX_EBIT_BOUNDS, reads hit 0
 instead and fails the call with TRAX_ERR_DEVICE_ASSERT.  The parity cases
-below run through it in a child process (TRAX_GB300_BOUNDS_CHECK=1 selects
+below (with the grid walk and the fine z grid walk of the prediction count)
+run through it in a child process (TRAX_GB300_BOUNDS_CHECK=1 selects
 the library): every call must finish without a bounds error and every array
 must equal the oracle's, as with the product build.
 """
@@ -36,9 +37,11 @@ CHILD = textwrap.dedent("""
     for name, batch in cases:
         ref = oracle.run(batch)[0]
         ctx.upload(batch)
-        for graph in (True, False):
+        for graph, fine in ((True, 0), (False, 0), (True, 4)):
+            ctx.set_fine_rows(fine)  # 4: the prediction count walks the fine z grid
             ctx.seed_batch(use_graph=graph)  # a bounds error raises TraxError here
             compare(ctx.results(), ref)
+        ctx.set_fine_rows(0)
         print(name, "clean", flush=True)
     compare(stagewise(ctx, events.generate(1)), oracle.run(events.generate(1))[0])
     print("stage by stage clean", flush=True)

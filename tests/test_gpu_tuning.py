@@ -127,6 +127,8 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
         assert entries[0]["pairs_per_thread"] == res["pairs_per_thread"]
         assert res["candidate_slots"] in (0, 4, 8, 16, 32)
         assert entries[0]["candidate_slots"] == res["candidate_slots"]
+        assert res["fine_rows"] in (0, 2, 4, 8, 16) and c.fine_rows() == res["fine_rows"]
+        assert entries[0]["fine_rows"] == res["fine_rows"]
     finally:
         c.close()
     # a new context with the same workload takes the cached shape without timing
@@ -136,7 +138,7 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
         res2 = c.autotune(cache_path=str(cache), search_grid=True, replays=1)
         assert res2["from_cache"] == 1 and res2["shapes_timed"] == 0
         keys = ("n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "pairs_per_thread",
-                "candidate_slots")
+                "candidate_slots", "fine_rows")
         assert [res2[k] for k in keys] == [res[k] for k in keys]
         # a different workload gets its own entry
         c.upload(events.generate(1, n_events=21))
@@ -148,8 +150,9 @@ def test_autotune_picks_a_shape_and_caches_it(trax_lib, oracle_lib, tmp_path):
 
 
 def test_autotune_cache_entry_without_pairs_per_thread(trax_lib, tmp_path):
-    """Cache files written before the pairs-per-thread and candidate-slot axes
-    existed still load (as 1 and the library's own choice)."""
+    """Cache files written before the pairs-per-thread, candidate-slot and
+    fine-grid axes existed still load (as 1, the library's own choice and no
+    fine grid)."""
     batch = events.generate(1, n_events=20)
     cache = tmp_path / "tune.json"
     c = trax_lib.Context(0)
@@ -160,11 +163,14 @@ def test_autotune_cache_entry_without_pairs_per_thread(trax_lib, tmp_path):
         for e in doc["entries"]:
             e.pop("pairs_per_thread")
             e.pop("candidate_slots")
+            e.pop("fine_rows")
         cache.write_text(json.dumps(doc))
         c.set_pairs_per_thread(4)
         c.set_candidate_slots(32)
+        c.set_fine_rows(8)
         res = c.autotune(cache_path=str(cache), search_grid=False, replays=1)
         assert res["from_cache"] == 1 and res["pairs_per_thread"] == 1 and c.pairs_per_thread() == 1
         assert res["candidate_slots"] == 0
+        assert res["fine_rows"] == 0 and c.fine_rows() == 0
     finally:
         c.close()

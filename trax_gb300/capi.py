@@ -37,6 +37,7 @@ EXPORTED = [
     "trax_host_free", "trax_set_wait_limit", "trax_debug_skip_publish", "trax_noalloc_set_wait",
     "trax_circle_fit_on", "trax_get_pt", "trax_cellular_automaton_on", "trax_set_pairs_per_thread",
     "trax_get_pairs_per_thread", "trax_math_eval", "trax_set_candidate_slots", "trax_get_candidate_slots",
+    "trax_set_fine_rows", "trax_get_fine_rows",
 ]
 
 
@@ -82,7 +83,7 @@ class TuneOptsC(ctypes.Structure):
 class TuneResultC(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint32) for n in (
         "n_z", "n_phi", "pair_threads", "predict_threads", "filter_threads", "from_cache", "shapes_timed",
-        "pairs_per_thread", "candidate_slots")] + [
+        "pairs_per_thread", "candidate_slots", "fine_rows", "reserved")] + [
         ("best_ms", ctypes.c_double), ("default_ms", ctypes.c_double)]
 
 
@@ -132,6 +133,8 @@ def load() -> ctypes.CDLL:
             "trax_get_pairs_per_thread": ([vp, vp], i32),
             "trax_set_candidate_slots": ([vp, u32], i32),
             "trax_get_candidate_slots": ([vp, vp], i32),
+            "trax_set_fine_rows": ([vp, u32], i32),
+            "trax_get_fine_rows": ([vp, vp], i32),
             "trax_set_wait_limit": ([vp, u32], i32),
             "trax_circle_fit_on": ([vp, vp, u64], i32),
             "trax_get_pt": ([vp, vp], i32),
@@ -383,6 +386,15 @@ class Context:
         """The number of captured candidates per pair in effect."""
         k = ctypes.c_uint32()
         self._check(self._L.trax_get_candidate_slots(self._h, ctypes.byref(k)))
+        return int(k.value)
+
+    def set_fine_rows(self, f: int):
+        """Rows of the prediction count's fine z grid per grid row (0: none, 2, 4, 8, 16)."""
+        self._check(self._L.trax_set_fine_rows(self._h, f))
+
+    def fine_rows(self) -> int:
+        k = ctypes.c_uint32()
+        self._check(self._L.trax_get_fine_rows(self._h, ctypes.byref(k)))
         return int(k.value)
 
     def pairs_per_thread(self) -> int:

@@ -112,6 +112,8 @@ struct trax_ctx {
   // candidates the prediction count captures per pair: keepSlots when the
   // caller set it, else keepAuto, chosen after each calibration
   uint32_t keepSlots = 0, keepAuto = TRAX_PRED_KEEP;
+  uint32_t fineRows = 0;  // rows of the prediction count's fine z grid per grid row (0: none)
+  uint32_t fineBuilt = 0;  // fineRows of the fine grid the last grid stage built
   bool haveLT = false, haveGeom = false, haveGrid = false, haveHits = false;
   bool cfgDirty = true;  // layer triplets or geometry changed since the device configuration was built
   // batch shape
@@ -130,6 +132,7 @@ struct trax_ctx {
       trk_counts;
   // grid stage
   DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
+  DevBuf fineGrid, fineZphi, fineCoarse;  // the fine z grid (fineRows > 0)
   // pair stage
   DevBuf segOuter, taskBase, taskCount, taskState, pairs, pairOffsets;
   // prediction / filter
@@ -250,6 +253,18 @@ DevHits dev_hits(trax_ctx* c) {
 
 uint32_t* slot(trax_ctx* c, int k) { return ptr<uint32_t>(c->slots) + k; }
 
+// The fine grid's buffers (to build it), and the fine grid the prediction
+// count may walk: only one the last grid stage built for the current
+// configuration (stages run one by one may change it in between).
+FineGrid fine_buffers(trax_ctx* c) {
+  if (!c->cfg.fineRows) return FineGrid{nullptr, nullptr, nullptr};
+  return FineGrid{ptr<uint32_t>(c->fineGrid), ptr<float2>(c->fineZphi), ptr<uint32_t>(c->fineCoarse)};
+}
+FineGrid fine_grid(trax_ctx* c) {
+  if (c->fineBuilt != c->cfg.fineRows) return FineGrid{nullptr, nullptr, nullptr};
+  return fine_buffers(c);
+}
+
 // A named NVTX range for the host side of a stage or call (what the
 // reference's per-run cl_event lists and RuntimeRecord classes show,
 // KernelWrapper.hpp:29-33, RuntimeRecord.cpp:123-192); free when no tool
@@ -320,6 +335,9 @@ int build_config(trax_ctx* c, bool seeding = true) {
   g.filterThreads = c->filterThreads;
   g.predPairsPerThread = c->predK;
   g.predKeep = c->keepSlots ? c->keepSlots : c->keepAuto;
+  g.fineRows = c->fineRows;
+  g.fineC = c->fineRows ? (c->fineRows * c->nZ + 1) * (c->nP + 1) : 0u;
+  g.fineScale = c->fineRows ? (float)c->fineRows / g.sZ : 0.0f;
   g.nHits = (uint32_t)c->nHits;
   g.err = slot(c, S_ERR);
   for (uint32_t p = 0; p < g.nLT; ++p) {
@@ -420,7 +438,18 @@ int stage_grid(trax_ctx* c, Mode mode) {
   ENSURE(player, n, 4); ENSURE(pdet, n, 4); ENSURE(phid, n, 4); ENSURE(pevt, n, 4); ENSURE(porig, n, 4);
   ENSURE(pxyzp, n, 16);
   ENSURE(sc_cell, n, 4); ENSURE(sc_phi, n, 4); ENSURE(sc_perm, n, 4);
-  if (c->cfg.C > TRAX_GRID_SMEM_CELLS) ENSURE(sc_counts, cells, 4);
+  uint64_t counters = c->cfg.C > TRAX_GRID_SMEM_CELLS ? cells : 0;
+  if (fine_counter_cells(c->cfg) > counters) counters = fine_counter_cells(c->cfg);
+  if (counters) ENSURE(sc_counts, counters, 4);
+  if (c->cfg.fineRows) {
+    ENSURE(fineGrid, (uint64_t)c->E * c->L * c->cfg.fineC, 4);
+    ENSURE(fineZphi, n, 8);
+    ENSURE(fineCoarse, n, 4);
+  } else if (mode == SYNCED) {  // switched off: give its memory back
+    release(c->fineGrid);
+    release(c->fineZphi);
+    release(c->fineCoarse);
+  }
   GridInput in;
   in.x = ptr<float>(c->in_x);
   in.y = ptr<float>(c->in_y);
@@ -440,6 +469,9 @@ int stage_grid(trax_ctx* c, Mode mode) {
   KBEG(TK_GRID);
   CK(grid_build(c->cfg, in, ptr<uint32_t>(c->grid), dev_hits(c), sc, c->maxLayerHits, dev_err(c), c->st,
                 &c->launches));
+  CK(fine_grid_build(c->cfg, ptr<uint32_t>(c->grid), ptr<float4>(c->pxyzp), fine_buffers(c), sc.counts, c->st,
+                     &c->launches));
+  c->fineBuilt = c->cfg.fineRows;
   KEND(TK_GRID);
   return TRAX_OK;
 }
@@ -495,14 +527,14 @@ int stage_predict(trax_ctx* c, Mode mode) {
   // warp the candidates' sum (scanned into the warp's first position)
   ENSURE(candLocal, maxPairs + 1, 4);
   ENSURE(predWarps, maxWarps + 1, 4);
-  ENSURE(predKeep, maxPairs * c->cfg.predKeep, 4);
+  ENSURE(predKeep, pred_keep_words(maxPairs, c->cfg.predKeep), 4);
   ENSURE(candOffsets, S + 1, 4);
   uint32_t* candLocal = ptr<uint32_t>(c->candLocal);
   uint32_t* warpSums = ptr<uint32_t>(c->predWarps);
   KBEG(TK_PRED_COUNT);
   CK(predict_pairs(c->cfg, false, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
                    candLocal, warpSums, slot(c, S_PRED_WARPS), ptr<uint32_t>(c->predKeep), nullptr, 0,
-                   slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+                   slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches, fine_grid(c)));
   KEND(TK_PRED_COUNT);
   // the prefix sum runs over the per-warp sums of the counts
   RC(scan_publish(c, mode, warpSums, (c->nPairs + 31) / 32, mode == DEVICE ? slot(c, S_PRED_WARPS) : nullptr,
@@ -772,7 +804,7 @@ int size_device_buffers(trax_ctx* c) {
   ENSURE(pairs, c->capPairs, 8);
   ENSURE(candLocal, c->capPairs + 1, 4);
   ENSURE(predWarps, (c->capPairs + 31) / 32 + 1, 4);
-  ENSURE(predKeep, c->capPairs * c->cfg.predKeep, 4);
+  ENSURE(predKeep, pred_keep_words(c->capPairs, c->cfg.predKeep), 4);
   ENSURE(cands, c->capCands, 8);
   ENSURE(flagWords, (c->capCands + 31) / 32 + 1, 4);
   ENSURE(flagSums, (c->capCands + 31) / 32 + 1, 4);
@@ -992,7 +1024,7 @@ void trax_destroy(trax_ctx* c) {
                     &c->trk_compStart, &c->trk_cursor, &c->trk_members, &c->trk_filtered, &c->trk_hits,
                     &c->trk_entryTrack, &c->trk_owner, &c->trk_table, &c->trk_counts, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
-                    &c->segOuter, &c->taskBase, &c->taskCount, &c->taskState, &c->pairs, &c->pairOffsets, &c->candLocal, &c->predWarps, &c->predKeep, &c->cands,
+                    &c->fineGrid, &c->fineZphi, &c->fineCoarse, &c->segOuter, &c->taskBase, &c->taskCount, &c->taskState, &c->pairs, &c->pairOffsets, &c->candLocal, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->linkRun, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS, &c->connW, &c->nonConnW,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,
@@ -1091,6 +1123,20 @@ int trax_set_candidate_slots(trax_ctx* c, uint32_t k) {
 int trax_get_candidate_slots(trax_ctx* c, uint32_t* k) {
   if (!c || !k) return TRAX_ERR_ARG;
   *k = c->keepSlots ? c->keepSlots : c->keepAuto;
+  return TRAX_OK;
+}
+
+int trax_set_fine_rows(trax_ctx* c, uint32_t f) {
+  if (!c) return TRAX_ERR_ARG;
+  if (f != 0 && f != 2 && f != 4 && f != 8 && f != 16)
+    return fail(c, TRAX_ERR_ARG, "fine rows must be 0 (none), 2, 4, 8 or 16");
+  c->fineRows = f;
+  return TRAX_OK;
+}
+
+int trax_get_fine_rows(trax_ctx* c, uint32_t* f) {
+  if (!c || !f) return TRAX_ERR_ARG;
+  *f = c->fineRows;
   return TRAX_OK;
 }
 
@@ -1265,6 +1311,7 @@ int trax_set_tracklets(trax_ctx* c, const uint32_t* h1, const uint32_t* h2, cons
   in.hid = ptr<uint32_t>(c->in_hid);
   in.evt = ptr<uint32_t>(c->in_evt);
   CK(identity_hits(in, (uint32_t)nh, dev_hits(c), c->st, &c->launches));
+  c->fineBuilt = 0;  // the hit collection is no longer the grid's
   if (n) {
     CK(cudaMemcpyAsync(c->h1.p, h1, n * 4, cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(c->h2.p, h2, n * 4, cudaMemcpyHostToDevice, c->st));

@@ -12,7 +12,10 @@
 // largest layer fits, else in global scratch.  It also writes
 // the packed (x, y, z, phi) array the candidate loops read with one 16-byte
 // load, phi being the same atan2 the cell assignment used.
+#include <algorithm>
+
 #include "trax_kernels.h"
+#include "trax_stages.cuh"
 
 namespace trax {
 
@@ -25,7 +28,61 @@ constexpr int GRID_WARPS = GRID_THREADS / 32;
 constexpr uint32_t GRID_SMEM_CELLS = TRAX_GRID_SMEM_CELLS;
 // dynamic shared memory a CTA may use: the counters plus, when they fit, the
 // cell, phi and slot of each of the layer's hits (12 bytes per hit)
-constexpr size_t GRID_SMEM_MAX = 227 * 1024 - 256;
+constexpr size_t GRID_SMEM_MAX = TRAX_GRID_SMEM_BYTES;
+
+// The CTA's exclusive scan of C cell counters in place: cnt[c] becomes the
+// first slot of cell c.  Each thread sums a chunk of consecutive cells,
+// warps scan the sums with shuffles, and the chunks are rewritten.
+__device__ __forceinline__ void cta_cell_scan(uint32_t* cnt, uint32_t C, uint32_t* s_warpSum) {
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t chunk = (C + GRID_THREADS - 1) / GRID_THREADS;
+  const uint32_t c0 = min(tid * chunk, C), c1 = min(c0 + chunk, C);
+  uint32_t local = 0;
+  for (uint32_t c = c0; c < c1; ++c) local += cnt[c];
+  uint32_t incl = local;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += t;
+  }
+  if (lane == 31) s_warpSum[warp] = incl;
+  __syncthreads();
+  uint32_t warpOff = 0;
+  for (uint32_t w = 0; w < warp; ++w) warpOff += s_warpSum[w];
+  uint32_t run = warpOff + incl - local;
+  __syncthreads();
+  for (uint32_t c = c0; c < c1; ++c) {
+    uint32_t v = cnt[c];
+    cnt[c] = run;  // becomes the next free slot of the cell
+    run += v;
+  }
+  __syncthreads();
+}
+
+// Stable placement of n hits by cell: a slot per hit from the cell cursors
+// cnt (atomics, any order inside a cell), then every cell's slots sorted by
+// the hits' positions i.  After the atomics cnt[c] is the end of cell c,
+// and so the start of cell c + 1.
+__device__ __forceinline__ void cta_place_stable(uint32_t* cnt, uint32_t C, const uint32_t* cellOf, uint32_t* perm,
+                                                 uint32_t n) {
+  const uint32_t tid = threadIdx.x;
+  for (uint32_t i = tid; i < n; i += GRID_THREADS) perm[atomicAdd(&cnt[cellOf[i]], 1u)] = i;
+  __syncthreads();
+  for (uint32_t c = tid; c < C; c += GRID_THREADS) {
+    const uint32_t lo = c ? cnt[c - 1] : 0u, hi = cnt[c];
+    if (hi - lo < 2) continue;
+    for (uint32_t a = lo + 1; a < hi; ++a) {  // insertion sort: cells hold a few hits
+      const uint32_t v = perm[a];
+      uint32_t b = a;
+      while (b > lo && perm[b - 1] > v) {
+        perm[b] = perm[b - 1];
+        --b;
+      }
+      perm[b] = v;
+    }
+  }
+  __syncthreads();
+}
 
 // The per-hit cell, phi and slot arrays are in shared memory after the
 // counters when the layer has at most maxHits hits (the room the launch
@@ -46,7 +103,7 @@ __global__ void __launch_bounds__(GRID_THREADS)
   uint32_t* cellOf = inSmem ? smem + C : sc.cell + base;
   float* phiOf = inSmem ? reinterpret_cast<float*>(smem + C + maxHits) : sc.phi + base;
   uint32_t* perm = inSmem ? smem + C + 2 * maxHits : sc.perm + base;
-  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const uint32_t tid = threadIdx.x;
 
   for (uint32_t c = tid; c < C; c += GRID_THREADS) cnt[c] = 0u;
   __syncthreads();
@@ -71,28 +128,7 @@ __global__ void __launch_bounds__(GRID_THREADS)
   __syncthreads();
 
   // 2. CTA exclusive scan of the counters; write the grid boundaries
-  const uint32_t chunk = (C + GRID_THREADS - 1) / GRID_THREADS;
-  const uint32_t c0 = min(tid * chunk, C), c1 = min(c0 + chunk, C);
-  uint32_t local = 0;
-  for (uint32_t c = c0; c < c1; ++c) local += cnt[c];
-  uint32_t incl = local;
-#pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= (uint32_t)d) incl += t;
-  }
-  if (lane == 31) s_warpSum[warp] = incl;
-  __syncthreads();
-  uint32_t warpOff = 0;
-  for (uint32_t w = 0; w < warp; ++w) warpOff += s_warpSum[w];
-  uint32_t run = warpOff + incl - local;
-  __syncthreads();
-  for (uint32_t c = c0; c < c1; ++c) {
-    uint32_t v = cnt[c];
-    cnt[c] = run;  // becomes the next free slot of the cell
-    run += v;
-  }
-  __syncthreads();
+  cta_cell_scan(cnt, C, s_warpSum);
   // the boundaries, written with consecutive threads on consecutive cells
   uint32_t* gl = grid + (size_t)task * C;
   for (uint32_t c = tid; c < C; c += GRID_THREADS) gl[c] = base + cnt[c];
@@ -101,24 +137,8 @@ __global__ void __launch_bounds__(GRID_THREADS)
   // 3. placement: a slot per hit from the cell cursors (shared-memory
   //    atomics, any order inside a cell), then every cell's slots sorted by
   //    input index -- the stable order, one of the orders the reference's
-  //    atomic_inc can produce.  After the atomics cnt[c] is the end of cell c,
-  //    and so the start of cell c + 1.
-  for (uint32_t i = tid; i < n; i += GRID_THREADS) perm[atomicAdd(&cnt[cellOf[i]], 1u)] = i;
-  __syncthreads();
-  for (uint32_t c = tid; c < C; c += GRID_THREADS) {
-    const uint32_t lo = c ? cnt[c - 1] : 0u, hi = cnt[c];
-    if (hi - lo < 2) continue;
-    for (uint32_t a = lo + 1; a < hi; ++a) {  // insertion sort: cells hold a few hits
-      const uint32_t v = perm[a];
-      uint32_t b = a;
-      while (b > lo && perm[b - 1] > v) {
-        perm[b] = perm[b - 1];
-        --b;
-      }
-      perm[b] = v;
-    }
-  }
-  __syncthreads();
+  //    atomic_inc can produce.
+  cta_place_stable(cnt, C, cellOf, perm, n);
 
   // 4. gather into cell order (gridStore, GridBuilder.h:243-253)
   for (uint32_t s = tid; s < n; s += GRID_THREADS) {
@@ -309,6 +329,85 @@ __global__ void __launch_bounds__(GRID_THREADS)
   }
 }
 
+// The fine z grid (fine_grid_build).  A hit's fine row lies in the block of
+// fineRows rows of its grid row, so the hits of one z row keep their range
+// [s0, s1) of grid order in fine order: every (event, layer, z row) is
+// sorted on its own, one warp each.  The warp counts the row's hits per
+// fine cell (fineRows x (nP + 1) cells: the block's rows, the grid's phi
+// columns), scans the counts into the fine grid's cell starts and places
+// the hits 32 at a time in grid order, each after the hits of its cell
+// before it (ranks among the lanes of equal cells), so ties keep grid
+// order.  A hit's grid row is the row whose range holds it, and its phi
+// column is recomputed with grid_kernel's operations on the same phi.
+// Counters in shared memory (warpsPerBlock blocks of cells) or, when one
+// block of cells does not fit, in global scratch.
+__device__ __forceinline__ uint32_t fine_cell(const DevConfig& cfg, float4 h, uint32_t r) {
+  const uint32_t s = fine_row(cfg, h.z, r) - r * cfg.fineRows;
+  const uint32_t col = min(f2u_sat(floor_(div_(h.w - cfg.minPhi, cfg.sP))), cfg.nP);
+  return s * (cfg.nP + 1) + col;
+}
+
+__global__ void __launch_bounds__(GRID_THREADS)
+    fine_grid_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ xyzp,
+                     FineGrid fine, uint32_t* gcnt, uint32_t warpsPerBlock) {
+  extern __shared__ uint32_t smem[];
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint32_t nZ = cfg.nZ, nP1 = cfg.nP + 1;
+  const uint32_t BC = cfg.fineRows * nP1;  // fine cells of one z row
+  const uint64_t task = (uint64_t)blockIdx.x * warpsPerBlock + wib;  // (event * L + layer) * nZ + row
+  if (wib >= warpsPerBlock || task >= (uint64_t)cfg.E * cfg.L * nZ) return;  // no block barrier follows
+  const uint32_t el = (uint32_t)(task / nZ), r = (uint32_t)(task % nZ);
+  const uint32_t* lG = grid + (size_t)el * cfg.C;
+  const uint32_t s0 = lG[r * nP1], s1 = lG[(r + 1) * nP1];
+  uint32_t* cnt = gcnt ? gcnt + task * BC : smem + wib * BC;
+  uint32_t* fG = fine.grid + (size_t)el * cfg.fineC + (size_t)r * BC;
+  for (uint32_t c = lane; c < BC; c += 32) cnt[c] = 0u;
+  __syncwarp();
+  for (uint32_t k = s0 + lane; k < s1; k += 32) atomicAdd(&cnt[fine_cell(cfg, xyzp[k], r)], 1u);
+  __syncwarp();
+  // exclusive scan, 32 cells at a time: the cell starts (positions of the batch)
+  uint32_t carry = s0;
+  for (uint32_t c0 = 0; c0 < BC; c0 += 32) {
+    const uint32_t c = c0 + lane;
+    const uint32_t v = c < BC ? cnt[c] : 0u;
+    uint32_t incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= (uint32_t)d) incl += t;
+    }
+    if (c < BC) {
+      cnt[c] = carry + incl - v;
+      fG[c] = carry + incl - v;
+    }
+    carry += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (r == nZ - 1)  // the row after the last holds no hit: its cells start at the layer's end
+    for (uint32_t c = lane; c < nP1; c += 32) fG[BC + c] = s1;
+  __syncwarp();
+  const uint32_t below = (1u << lane) - 1u;
+  for (uint32_t k0 = s0; k0 < s1; k0 += 32) {
+    const uint32_t k = k0 + lane;
+    const bool active = k < s1;
+    const uint32_t mask = __ballot_sync(0xffffffffu, active);
+    float4 h = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint32_t cell = 0, peers = 0, pos = 0;
+    if (active) {
+      h = xyzp[k];
+      cell = fine_cell(cfg, h, r);
+      peers = __match_any_sync(mask, cell);
+      pos = cnt[cell] + __popc(peers & below);
+    }
+    __syncwarp();
+    if (active) {
+      if ((peers & below) == 0u) cnt[cell] += __popc(peers);  // the lowest lane of the cell moves its cursor
+      fine.zphi[pos] = make_float2(h.z, h.w);
+      fine.coarse[pos] = k;
+    }
+    __syncwarp();
+  }
+}
+
 // The uploaded hits taken as the hit collection as they are (identity
 // order), for the linking stages run on caller-provided triplets.
 __global__ void identity_hits_kernel(GridInput in, uint32_t n, DevHits out) {
@@ -338,7 +437,9 @@ cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStre
 cudaError_t grid_prepare(int) {
   cudaError_t e = cudaFuncSetAttribute(grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(grid_kernel16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
+  e = cudaFuncSetAttribute(grid_kernel16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(fine_grid_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRID_SMEM_MAX);
 }
 
 cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid, DevHits out, GridScratch sc,
@@ -358,6 +459,21 @@ cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid
   const bool hitsFit = useSmem && counterBytes + hitBytes <= GRID_SMEM_MAX;
   grid_kernel<<<tasks, GRID_THREADS, counterBytes + (hitsFit ? hitBytes : 0), st>>>(
       cfg, in, grid, out, sc, err, useSmem, hitsFit ? maxLayerHits : 0u);
+  if (launches) *launches += 1;
+  return cudaGetLastError();
+}
+
+cudaError_t fine_grid_build(const DevConfig& cfg, const uint32_t* grid, const float4* xyzp, FineGrid fine,
+                            uint32_t* counters, cudaStream_t st, uint32_t* launches) {
+  const uint64_t tasks = (uint64_t)cfg.E * cfg.L * cfg.nZ;
+  if (tasks == 0 || cfg.fineRows == 0) return cudaSuccess;
+  const size_t rowBytes = (size_t)fine_row_cells(cfg) * sizeof(uint32_t);
+  uint32_t wpb = (uint32_t)std::min<size_t>(GRID_WARPS, GRID_SMEM_MAX / rowBytes);
+  const bool inSmem = wpb > 0;
+  if (!inSmem) wpb = GRID_WARPS;
+  const uint64_t blocks = (tasks + wpb - 1) / wpb;
+  fine_grid_kernel<<<(unsigned)blocks, wpb * 32, inSmem ? wpb * rowBytes : 0, st>>>(cfg, grid, xyzp, fine,
+                                                                                     inSmem ? nullptr : counters, wpb);
   if (launches) *launches += 1;
   return cudaGetLastError();
 }

@@ -29,6 +29,91 @@ int grid_for(uint64_t items, int threads) {
   return (int)blocks;
 }
 
+// The count pass's walk over the fine z grid (cfg.fineRows rows per z row),
+// for windows with pL <= nP.  It visits the same hits as the walk over the
+// grid, each as often, so the counts are the same:
+//  - the grid walk visits, in each z row r of [zLo, zHi), the hits of the
+//    row's phi columns [pL, pH) (no wrap), or [pL, nP] and then [0, pH)
+//    (wrap; both parts when pH > pL, so such hits twice) -- pred_row_parts
+//    for pL <= nP, with pH <= nP always;
+//  - here, for each of r's parts, the fine rows of r's block that meet
+//    [fine_row(zl), fine_row(zh)], the union window's bounds; a hit passing
+//    either variant's z test has zl <= z <= zh, and fine_row is monotone
+//    and keeps it in its grid row's block, so its fine row is among them.
+//    Hits outside those rows fail both z tests, as in the grid walk.
+// The captured candidates are the first predKeep store-valid visits in the
+// grid walk's order, (row, part, grid index): the visits of one (row, part)
+// come here in fine order, so the slots of the current (row, part) are kept
+// sorted by grid index -- appended while they come in order (the largest
+// is kept in a register), inserted otherwise -- and a visit past the last
+// slot replaces the largest of them when it is smaller.
+template <class Slots>
+__device__ __forceinline__ void fine_walk(const DevConfig& cfg, const PredUnionWindow& w, const FineGrid& fine,
+                                          uint32_t event, uint32_t layer, Slots slot, uint32_t& count,
+                                          uint32_t& nStore) {
+  const uint32_t F = cfg.fineRows, Cf = cfg.fineC, nP = cfg.nP;
+  const uint32_t nKeep = cfg.predKeep;
+  const uint32_t* lG = fine.grid + ((size_t)event * cfg.L + layer) * Cf;
+  // zl, zh as pred_union_window (a switched-off variant holds +inf, -inf);
+  // their grid rows are min(zLo, nZ - 1) and zHi - 1 (zHi >= 1 when any)
+  const float zl = fminf(w.zLow[0], w.zLow[1]), zh = fmaxf(w.zHigh[0], w.zHigh[1]);
+  const uint32_t fLo = fine_row(cfg, zl, min(w.zLo, cfg.nZ - 1u));
+  const uint32_t fHi = w.zHi ? fine_row(cfg, zh, w.zHi - 1u) + 1u : 0u;
+  const bool wrap = w.wrap != 0u;
+  const float zl0 = w.zLow[0], zh0 = w.zHigh[0], zl1 = w.zLow[1], zh1 = w.zHigh[1];
+  for (uint32_t r = w.zLo; r < w.zHi; ++r) {
+    const uint32_t f0 = max(F * r, fLo), f1 = min(F * r + F, fHi);
+    for (uint32_t part = 0; part <= w.wrap; ++part) {
+      const uint32_t cs = nStore;  // the first visit of this (row, part)
+      uint32_t last = 0u;          // the largest kept of this (row, part), at min(nStore, nKeep) - 1
+      // part 0: columns [pL, pH), or [pL, nP] under wrap; part 1: [0, pH)
+      const uint32_t ca = part ? 0u : w.pL;
+      const uint32_t cb = (wrap && !part) ? nP + 1u : w.pH;
+      for (uint32_t fr = f0; fr < f1; ++fr) {
+        const uint32_t row = fr * (nP + 1u);
+        const uint32_t a = cell_at(lG, row + ca, Cf);
+        const uint32_t b = max(a, cell_at(lG, row + cb, Cf));
+#pragma unroll 1  // a few hits per fine row: unrolled by 4 it measured slower (12.8 vs 12.4 ms)
+        for (uint32_t jf = a; jf < b; ++jf) {
+          const float2 h = __ldg(fine.zphi + trax_hit(jf, cfg));
+          const bool lo = w.phiLow <= h.y, hi = h.y <= w.phiHigh;
+          const bool phiOk = wrap ? (lo || hi) : (lo && hi);
+          count += (phiOk && zl0 <= h.x && h.x <= zh0);
+          if (phiOk && zl1 <= h.x && h.x <= zh1) {
+            const uint32_t j = __ldg(fine.coarse + trax_hit(jf, cfg));
+            if (nStore < nKeep) {
+              if (nStore == cs || j > last) {  // in grid order: append
+                slot[nStore] = j;
+                last = j;
+              } else {  // before `last`: move the larger ones up (the largest stays `last`)
+                uint32_t q = nStore;
+                slot[q--] = last;
+                while (q > cs && slot[q - 1u] > j) {
+                  slot[q] = slot[q - 1u];
+                  --q;
+                }
+                slot[q] = j;
+              }
+            } else if (cs < nKeep && j < last) {  // replaces the largest kept, at nKeep - 1
+              uint32_t q = nKeep - 1u, top = j;
+              while (q > cs) {
+                const uint32_t v = slot[q - 1u];
+                if (v <= j) break;
+                slot[q] = v;
+                if (q == nKeep - 1u) top = v;
+                --q;
+              }
+              slot[q] = j;
+              last = top;
+            }
+            ++nStore;
+          }
+        }
+      }
+    }
+  }
+}
+
 // Count pass (predictCount, :190-219) that also captures the first
 // min(count, cfg.predKeep) candidates the store pass would write (the store
 // variant's valid hits, capped at the count; slots it would leave unwritten
@@ -40,11 +125,15 @@ int grid_for(uint64_t items, int threads) {
 // pair's position is its warp's scanned sum plus its offset in the warp.
 // At most 40 registers (six blocks of 256 threads per SM), where it spills
 // nothing; 32 registers (eight blocks) spill and measured slower, as did 48.
+//
+// FINE: the walk goes over the fine z grid instead (fine_walk), with the
+// same counts and captured candidates.  IL: the slots' layout (keep_slots).
+template <bool FINE, bool IL>
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
     predict_count_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
                          const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev, uint32_t* candCount,
-                         uint32_t* keep, uint32_t* warpSums, uint32_t* nWarpsOut, uint32_t* err) {
+                         uint32_t* keep, uint32_t* warpSums, uint32_t* nWarpsOut, uint32_t* err, FineGrid fine) {
   const uint32_t nPairs = *nPairsDev;
   const uint32_t lane = threadIdx.x & 31u;
   // warp-uniform loop: each warp covers 32 consecutive pairs per step
@@ -66,7 +155,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
       // hits come out in its own visit order.
       const uint32_t C = cfg.C, nP = cfg.nP;
       const uint32_t nKeep = cfg.predKeep;
-      uint32_t* slot = keep + (size_t)gid * nKeep;
+      const KeepSlots<IL, uint32_t> slot = keep_slots<IL>(keep, gid, nKeep);
       uint32_t nStore = 0;
       // The phi test (TripletThetaPhiPredictor.h:211-214) on hit angles
       // from atan2_, which lie in [-pi, pi] or are NaN: the wrapped window's
@@ -75,6 +164,9 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
       const bool wrap = w.wrap != 0u;
       const float zl0 = w.zLow[0], zh0 = w.zHigh[0], zl1 = w.zLow[1], zh1 = w.zHigh[1];
       const float2* zphi = reinterpret_cast<const float2*>(hits) + 1;  // (z, phi) of hit j at zphi[2 j]
+      if (FINE && w.pL <= nP) {
+        fine_walk(cfg, w, fine, event, layer, slot, count, nStore);
+      } else
       for (uint32_t zs = w.zLo; zs < w.zHi; ++zs) {
         uint32_t a[2], b[2];
         pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
@@ -195,7 +287,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
     PredWindow rw;  // pL, pH and wrap for pred_row_parts
     rw.pL = rw.pH = rw.wrap = 0;
     const uint32_t* lG3 = grid;
-    uint32_t* slot = keep;
+    KeepSlots<false, uint32_t> slot{keep};
     uint32_t counts[K];
 #pragma unroll
     for (int q = 0; q < K; ++q) counts[q] = 0;
@@ -242,7 +334,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
             pa2 = rw.wrap ? -TRAX_PI_F : inf;
             pb2 = rw.wrap ? ps.phiHigh : -inf;
             lG3 = grid + ps.gridOff;
-            slot = keep + (size_t)(base + 32u * k + lane) * cfg.predKeep;
+            slot = keep_slots<false>(keep, base + 32u * k + lane, cfg.predKeep);
             zs = min(zlo[0], zlo[1]);
             zHi = max(zhi[0], zhi[1]);
             if (zs < zHi) break;
@@ -312,6 +404,8 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
 // pair has more candidates than slots.
 // At most 32 registers: full occupancy hides the latency of the dependent
 // loads better than the few spilled bytes cost (0.61 -> 0.49 ms).
+// IL: the slots' layout (keep_slots).
+template <bool IL>
 __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
     predict_store_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
@@ -331,7 +425,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
     if (limit == 0) continue;
     uint2* out = cands + pos;
     if (limit <= cfg.predKeep) {
-      const uint32_t* slot = keep + (size_t)gid * cfg.predKeep;
+      const KeepSlots<IL, const uint32_t> slot = keep_slots<IL>(keep, gid, cfg.predKeep);
       for (uint32_t q = 0; q < limit; ++q) {
         const uint32_t h = slot[q];
         sent += h == TRAX_SENTINEL;
@@ -587,17 +681,33 @@ bool pred_k_fits(const DevConfig& cfg) {
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
                           const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* warpSums,
                           uint32_t* nWarpsOut, uint32_t* keep, uint2* cands, uint64_t capCands, uint32_t* sentinels,
-                          uint32_t* err, cudaStream_t st, uint32_t* launches) {
+                          uint32_t* err, cudaStream_t st, uint32_t* launches, FineGrid fine) {
   const uint32_t cap = capCands > 0xffffffffull ? 0xffffffffu : (uint32_t)capCands;
   const int threads = (int)cfg.predThreads;
   const int blocks = grid_for(maxPairs + 1, threads);
+  const bool il = keep_interleaved(cfg);
   if (emit) {
     if (maxPairs == 0) return cudaSuccess;
-    predict_store_kernel<<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                          nPairsDev, candCount, warpSums, keep, cands, cap, sentinels);
+    if (il)
+      predict_store_kernel<true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+                                                             nPairsDev, candCount, warpSums, keep, cands, cap,
+                                                             sentinels);
+    else
+      predict_store_kernel<false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+                                                              nPairsDev, candCount, warpSums, keep, cands, cap,
+                                                              sentinels);
+  } else if (cfg.fineRows > 0 && fine.grid) {
+    predict_count_kernel<true, true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+                                                                 nPairsDev, candCount, keep, warpSums, nWarpsOut,
+                                                                 err, fine);
+  } else if (il) {  // the K-pairs kernel keeps the consecutive layout
+    predict_count_kernel<false, true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
+                                                                  nPairsDev, candCount, keep, warpSums, nWarpsOut,
+                                                                  err, fine);
   } else if (cfg.predPairsPerThread <= 1 || !pred_k_fits(cfg)) {
-    predict_count_kernel<<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                          nPairsDev, candCount, keep, warpSums, nWarpsOut, err);
+    predict_count_kernel<false, false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer,
+                                                                   pairs, nPairsDev, candCount, keep, warpSums,
+                                                                   nWarpsOut, err, fine);
   } else {
     const int K = cfg.predPairsPerThread;
     const size_t smem = (size_t)threads * K * sizeof(PredStage);

@@ -39,6 +39,10 @@ struct DevConfig {
   uint32_t pairThreads, predThreads, filterThreads;
   uint32_t predPairsPerThread;  // 1, 2 or 4 pairs per thread in the prediction count pass
   uint32_t predKeep;            // candidates captured per pair by the count pass (4, 8, 16 or 32)
+  // fine z grid of the prediction count: fineRows rows per z row of the grid
+  // (0: none), fineC cells per (event, layer), fineScale = fineRows / sZ
+  uint32_t fineRows, fineC;
+  float fineScale;
   uint32_t nHits;               // hits of the batch (the length of every per-hit array)
   uint32_t* err;                // the context's device error word
 };

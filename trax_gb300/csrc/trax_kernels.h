@@ -129,6 +129,31 @@ cudaError_t grid_build(const DevConfig& cfg, const GridInput& in, uint32_t* grid
                        GridScratch scratch, uint32_t maxLayerHits, uint32_t* err, cudaStream_t st,
                        uint32_t* launches);
 cudaError_t grid_prepare(int device);  // one-time kernel attributes
+
+// The fine z grid the prediction count walks when cfg.fineRows > 0: the
+// grid-ordered hits of every (event, layer) sorted again by fine cell (fine
+// row = fine_row of the hit's z inside its z row's block of fineRows rows,
+// the same phi column), ties by grid order.  grid[E*L*fineC] holds the
+// cell starts like the grid's, zphi[n] the (z, phi) and coarse[n] the
+// grid-order index of each hit in fine order.  Built from the grid and the
+// grid-ordered packed hits (xyzp) after grid_build; `counters` (global
+// scratch of fine_counter_cells(cfg) words) is used only when one z row's
+// fine cells do not fit in shared memory.
+struct FineGrid {
+  uint32_t* grid;
+  float2* zphi;
+  uint32_t* coarse;
+};
+// dynamic shared memory the grid builds give one CTA
+#define TRAX_GRID_SMEM_BYTES (227u * 1024u - 256u)
+inline uint32_t fine_row_cells(const DevConfig& cfg) { return cfg.fineRows * (cfg.nP + 1); }
+inline uint64_t fine_counter_cells(const DevConfig& cfg) {
+  return (uint64_t)fine_row_cells(cfg) * sizeof(uint32_t) > TRAX_GRID_SMEM_BYTES
+             ? (uint64_t)cfg.E * cfg.L * cfg.nZ * fine_row_cells(cfg)
+             : 0;
+}
+cudaError_t fine_grid_build(const DevConfig& cfg, const uint32_t* grid, const float4* xyzp, FineGrid fine,
+                            uint32_t* counters, cudaStream_t st, uint32_t* launches);
 // hit collection = uploaded hits in input order (plus the packed xyz-phi array)
 cudaError_t identity_hits(const GridInput& in, uint32_t n, DevHits out, cudaStream_t st, uint32_t* launches);
 
@@ -178,14 +203,21 @@ cudaError_t pair_offsets(const DevConfig& cfg, const uint32_t* taskBase, const u
 // the default) to TRAX_PRED_KEEP_MAX.
 #define TRAX_PRED_KEEP 4
 #define TRAX_PRED_KEEP_MAX 32
+// words of the captured candidates of `pairs` pairs, whole warps of 32
+// pairs; the slots of a warp's pairs are interleaved (keep_slots) with 16 or
+// more slots per pair or with the fine z grid
+inline uint64_t pred_keep_words(uint64_t pairs, uint32_t keep) { return (pairs + 31) / 32 * 32 * keep; }
+inline bool keep_interleaved(const DevConfig& cfg) { return cfg.predKeep >= 16u || cfg.fineRows > 0u; }
 
 // grids of up to this many cells per layer are built with shared-memory
 // counters (4 bytes per cell)
 #define TRAX_GRID_SMEM_CELLS 53248u
+// With cfg.fineRows > 0 the count pass walks `fine` (same outputs).
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
                           const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* warpSums,
                           uint32_t* nWarpsOut, uint32_t* keep, uint2* cands, uint64_t capCands,
-                          uint32_t* sentinelCount, uint32_t* err, cudaStream_t st, uint32_t* launches);
+                          uint32_t* sentinelCount, uint32_t* err, cudaStream_t st, uint32_t* launches,
+                          FineGrid fine = FineGrid{nullptr, nullptr, nullptr});
 cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, const uint32_t* nPairsDev,
                             const uint32_t* candCount, const uint32_t* warpStart, uint32_t* candOffsets,
                             cudaStream_t st, uint32_t* launches);

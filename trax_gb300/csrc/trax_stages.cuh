@@ -39,6 +39,36 @@ __device__ __forceinline__ uint32_t pred_row_hi_raw(const DevConfig& cfg, float 
   return f2u_sat(floor_(div_(zHigh - cfg.minZ, cfg.sZ)));
 }
 
+// The candidates the prediction count captures for pair gid, slot q at
+// p[q * stride].  Interleaved (IL, keep_interleaved: 16 or more slots per
+// pair, or the fine z grid), the slots of a warp's 32 consecutive pairs
+// share lines (stride 32: slot q of those pairs is one 128-byte line, which
+// the lanes fill and read together); otherwise a pair's slots are
+// consecutive (stride 1: one or two 32-byte sectors per pair, mostly
+// holding one candidate).  The layout is a template parameter of the
+// kernels that touch the slots, chosen on the host.
+template <bool IL, class T>
+struct KeepSlots {
+  T* p;
+  __device__ __forceinline__ T& operator[](uint32_t q) const { return p[(size_t)q * (IL ? 32u : 1u)]; }
+};
+template <bool IL, class T>
+__device__ __forceinline__ KeepSlots<IL, T> keep_slots(T* keep, uint32_t gid, uint32_t nKeep) {
+  return KeepSlots<IL, T>{IL ? keep + (((size_t)(gid >> 5) * nKeep) << 5) + (gid & 31u) : keep + (size_t)gid * nKeep};
+}
+
+// Row of z in the fine grid, given G, z's row in the grid clamped to
+// [0, nZ): h = floor((z - minZ) * fineScale) clamped into G's block
+// [G fineRows, G fineRows + fineRows).  Both h and G are non-decreasing in
+// z, so the fine row is too (a larger G puts it in a later block, an equal
+// G clamps a larger h into the same block), and a hit's fine row lies in
+// the block of its grid row.
+__device__ __forceinline__ uint32_t fine_row(const DevConfig& cfg, float z, uint32_t G) {
+  const uint32_t h = f2u_sat(floor_((z - cfg.minZ) * cfg.fineScale));
+  const uint32_t lo = G * cfg.fineRows;
+  return min(max(h, lo), lo + cfg.fineRows - 1u);
+}
+
 __device__ __forceinline__ void pred_z_window(const DevConfig& cfg, float p1z, float p2z, float rOrigin,
                                               float r2t, float tip2, float minR, float maxR, float sigmaZ,
                                               float& zLow, float& zHigh, uint32_t& lo, uint32_t& hi) {

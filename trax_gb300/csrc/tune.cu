@@ -5,8 +5,9 @@
 // call of a shape calibrates and captures, the replays are timed with CUDA
 // events on the context's stream) and keeps the fastest.  The grid is
 // searched first with the current block sizes, then each kernel's block size
-// in turn.  Results go to a small JSON cache keyed by the workload hash and
-// the SM count.
+// in turn, then the prediction count's pairs per thread, captured candidate
+// slots and fine z grid.  Results go to a small JSON cache keyed by the
+// workload hash and the SM count.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +27,7 @@ struct Shape {
   uint32_t nZ, nP, pairT, predT, filtT;
   uint32_t predK;  // pairs per thread of the prediction count
   uint32_t slots;  // candidates it captures per pair (0: the library's choice)
+  uint32_t fine;   // rows of its fine z grid per grid row (0: none)
 };
 
 int apply_shape(trax_ctx* c, const Shape& s) {
@@ -33,6 +35,7 @@ int apply_shape(trax_ctx* c, const Shape& s) {
   if (rc == TRAX_OK) rc = trax_set_block_sizes(c, s.pairT, s.predT, s.filtT);
   if (rc == TRAX_OK) rc = trax_set_pairs_per_thread(c, s.predK);
   if (rc == TRAX_OK) rc = trax_set_candidate_slots(c, s.slots);
+  if (rc == TRAX_OK) rc = trax_set_fine_rows(c, s.fine);
   return rc;
 }
 
@@ -125,11 +128,12 @@ bool cache_lookup(const char* path, const std::string& key, Shape* s, double* ms
     if (!field_u64(e, "n_z", &v[0]) || !field_u64(e, "n_phi", &v[1]) || !field_u64(e, "pair_threads", &v[2]) ||
         !field_u64(e, "predict_threads", &v[3]) || !field_u64(e, "filter_threads", &v[4]))
       continue;
-    unsigned long long ppt = 1, slots = 0;  // entries written before these axes existed
+    unsigned long long ppt = 1, slots = 0, fine = 0;  // entries written before these axes existed
     field_u64(e, "pairs_per_thread", &ppt);
     field_u64(e, "candidate_slots", &slots);
+    field_u64(e, "fine_rows", &fine);
     *s = Shape{(uint32_t)v[0], (uint32_t)v[1], (uint32_t)v[2], (uint32_t)v[3], (uint32_t)v[4], (uint32_t)ppt,
-               (uint32_t)slots};
+               (uint32_t)slots, (uint32_t)fine};
     if (!field_f64(e, "ms", ms)) *ms = 0.0;
     return true;
   }
@@ -146,8 +150,8 @@ bool cache_store(const char* path, const std::string& key, int sms, const Shape&
   snprintf(b, sizeof(b),
            "{\"key\": \"%s\", \"sm_count\": %d, \"n_z\": %u, \"n_phi\": %u, \"pair_threads\": %u, "
            "\"predict_threads\": %u, \"filter_threads\": %u, \"pairs_per_thread\": %u, "
-           "\"candidate_slots\": %u, \"ms\": %.6f}",
-           key.c_str(), sms, s.nZ, s.nP, s.pairT, s.predT, s.filtT, s.predK, s.slots, ms);
+           "\"candidate_slots\": %u, \"fine_rows\": %u, \"ms\": %.6f}",
+           key.c_str(), sms, s.nZ, s.nP, s.pairT, s.predT, s.filtT, s.predK, s.slots, s.fine, ms);
   keep.push_back(b);
   const std::string tmp = std::string(path) + ".tmp";
   {
@@ -180,12 +184,13 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, trax::ctx_device(c));
 
-  uint32_t cur[5], curK = 1;
+  uint32_t cur[5], curK = 1, curF = 0;
   int rc = trax_get_launch_config(c, cur);
   if (rc == TRAX_OK) rc = trax_get_pairs_per_thread(c, &curK);
+  if (rc == TRAX_OK) rc = trax_get_fine_rows(c, &curF);
   if (rc != TRAX_OK) return rc;
   // the capture slots start from the library's own choice
-  const Shape start{cur[0], cur[1], cur[2], cur[3], cur[4], curK, 0u};
+  const Shape start{cur[0], cur[1], cur[2], cur[3], cur[4], curK, 0u, curF};
 
   uint64_t h = trax::workload_hash(c);
   h ^= (uint64_t)sms * 0x9e3779b97f4a7c15ull;
@@ -226,7 +231,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
         for (uint32_t p : ps) {
           if ((z + 1) * (p + 1) > TRAX_GRID_SMEM_CELLS) continue;
           if (z == start.nZ && p == start.nP) continue;
-          consider(Shape{z, p, best.pairT, best.predT, best.filtT, best.predK, best.slots});
+          consider(Shape{z, p, best.pairT, best.predT, best.filtT, best.predK, best.slots, best.fine});
         }
     }
     static const uint32_t ts[] = {64, 96, 128, 192, 256};
@@ -255,6 +260,15 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
       s.slots = k;
       consider(s);
     }
+    // then the fine z grid of the prediction count
+    static const uint32_t fineChoices[] = {0, 2, 4, 8, 16};
+    const Shape bySlots = best;
+    for (uint32_t f : fineChoices) {
+      if (f == bySlots.fine) continue;
+      Shape s = bySlots;
+      s.fine = f;
+      consider(s);
+    }
     rc = apply_shape(c, best);
     if (rc != TRAX_OK) return rc;
     res.best_ms = bestMs;
@@ -270,6 +284,7 @@ extern "C" int trax_autotune(trax_ctx* c, const char* cache_path, const trax_tun
   res.filter_threads = best.filtT;
   res.pairs_per_thread = best.predK;
   res.candidate_slots = best.slots;
+  res.fine_rows = best.fine;
   if (result) *result = res;
   return TRAX_OK;
 }
