@@ -132,7 +132,7 @@ struct trax_ctx {
       trk_counts;
   // grid stage
   DevBuf grid, px, py, pz, player, pdet, phid, pevt, porig, pxyzp, sc_cell, sc_phi, sc_perm, sc_counts;
-  DevBuf fineGrid, fineZphi, fineCoarse;  // the fine z grid (fineRows > 0)
+  DevBuf fineGrid, fineHits;  // the fine z grid (fineRows > 0)
   // pair stage
   DevBuf segOuter, taskBase, taskCount, taskState, pairs, pairOffsets;
   // prediction / filter
@@ -257,11 +257,11 @@ uint32_t* slot(trax_ctx* c, int k) { return ptr<uint32_t>(c->slots) + k; }
 // count may walk: only one the last grid stage built for the current
 // configuration (stages run one by one may change it in between).
 FineGrid fine_buffers(trax_ctx* c) {
-  if (!c->cfg.fineRows) return FineGrid{nullptr, nullptr, nullptr};
-  return FineGrid{ptr<uint32_t>(c->fineGrid), ptr<float2>(c->fineZphi), ptr<uint32_t>(c->fineCoarse)};
+  if (!c->cfg.fineRows) return FineGrid{nullptr, nullptr};
+  return FineGrid{ptr<uint32_t>(c->fineGrid), ptr<float4>(c->fineHits)};
 }
 FineGrid fine_grid(trax_ctx* c) {
-  if (c->fineBuilt != c->cfg.fineRows) return FineGrid{nullptr, nullptr, nullptr};
+  if (c->fineBuilt != c->cfg.fineRows) return FineGrid{nullptr, nullptr};
   return fine_buffers(c);
 }
 
@@ -443,12 +443,10 @@ int stage_grid(trax_ctx* c, Mode mode) {
   if (counters) ENSURE(sc_counts, counters, 4);
   if (c->cfg.fineRows) {
     ENSURE(fineGrid, (uint64_t)c->E * c->L * c->cfg.fineC, 4);
-    ENSURE(fineZphi, n, 8);
-    ENSURE(fineCoarse, n, 4);
+    ENSURE(fineHits, n, 16);
   } else if (mode == SYNCED) {  // switched off: give its memory back
     release(c->fineGrid);
-    release(c->fineZphi);
-    release(c->fineCoarse);
+    release(c->fineHits);
   }
   GridInput in;
   in.x = ptr<float>(c->in_x);
@@ -1024,7 +1022,7 @@ void trax_destroy(trax_ctx* c) {
                     &c->trk_compStart, &c->trk_cursor, &c->trk_members, &c->trk_filtered, &c->trk_hits,
                     &c->trk_entryTrack, &c->trk_owner, &c->trk_table, &c->trk_counts, &c->grid, &c->px, &c->py, &c->pz, &c->player, &c->pdet, &c->phid,
                     &c->pevt, &c->porig, &c->pxyzp, &c->sc_cell, &c->sc_phi, &c->sc_perm, &c->sc_counts,
-                    &c->fineGrid, &c->fineZphi, &c->fineCoarse, &c->segOuter, &c->taskBase, &c->taskCount, &c->taskState, &c->pairs, &c->pairOffsets, &c->candLocal, &c->predWarps, &c->predKeep, &c->cands,
+                    &c->fineGrid, &c->fineHits, &c->segOuter, &c->taskBase, &c->taskCount, &c->taskState, &c->pairs, &c->pairOffsets, &c->candLocal, &c->predWarps, &c->predKeep, &c->cands,
                     &c->candOffsets, &c->flagWords, &c->flagSums, &c->h1, &c->h2, &c->h3, &c->tripOffsets, &c->eta, &c->segOf,
                     &c->segStart, &c->linkCount, &c->linkRun, &c->cflags, &c->basis, &c->follower, &c->connS, &c->nonConnS, &c->connW, &c->nonConnW,
                     &c->connIdx, &c->nonConnIdx, &c->pt, &c->states, &c->inStart, &c->inCursor, &c->inList, &c->best,

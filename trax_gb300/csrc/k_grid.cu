@@ -401,8 +401,7 @@ __global__ void __launch_bounds__(GRID_THREADS)
     __syncwarp();
     if (active) {
       if ((peers & below) == 0u) cnt[cell] += __popc(peers);  // the lowest lane of the cell moves its cursor
-      fine.zphi[pos] = make_float2(h.z, h.w);
-      fine.coarse[pos] = k;
+      fine.hits[pos] = make_float4(h.z, h.w, __uint_as_float(k), 0.0f);
     }
     __syncwarp();
   }

@@ -134,15 +134,15 @@ cudaError_t grid_prepare(int device);  // one-time kernel attributes
 // grid-ordered hits of every (event, layer) sorted again by fine cell (fine
 // row = fine_row of the hit's z inside its z row's block of fineRows rows,
 // the same phi column), ties by grid order.  grid[E*L*fineC] holds the
-// cell starts like the grid's, zphi[n] the (z, phi) and coarse[n] the
-// grid-order index of each hit in fine order.  Built from the grid and the
+// cell starts like the grid's, hits[n] each hit in fine order as (z, phi,
+// its grid-order index as the bits of a float, 0): one 16-byte load gives
+// a visit its test and its candidate.  Built from the grid and the
 // grid-ordered packed hits (xyzp) after grid_build; `counters` (global
 // scratch of fine_counter_cells(cfg) words) is used only when one z row's
 // fine cells do not fit in shared memory.
 struct FineGrid {
   uint32_t* grid;
-  float2* zphi;
-  uint32_t* coarse;
+  float4* hits;
 };
 // dynamic shared memory the grid builds give one CTA
 #define TRAX_GRID_SMEM_BYTES (227u * 1024u - 256u)
@@ -217,7 +217,7 @@ cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid,
                           const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* warpSums,
                           uint32_t* nWarpsOut, uint32_t* keep, uint2* cands, uint64_t capCands,
                           uint32_t* sentinelCount, uint32_t* err, cudaStream_t st, uint32_t* launches,
-                          FineGrid fine = FineGrid{nullptr, nullptr, nullptr});
+                          FineGrid fine = FineGrid{nullptr, nullptr});
 cudaError_t predict_offsets(const DevConfig& cfg, const uint32_t* pairOffsets, const uint32_t* nPairsDev,
                             const uint32_t* candCount, const uint32_t* warpStart, uint32_t* candOffsets,
                             cudaStream_t st, uint32_t* launches);
