@@ -546,7 +546,7 @@ int stage_predict(trax_ctx* c, Mode mode) {
   KBEG(TK_PRED_EMIT);
   CK(predict_pairs(c->cfg, true, ptr<uint32_t>(c->grid), dev_hits(c), ptr<uint2>(c->pairs), nPairsDev, maxPairs,
                    candLocal, warpSums, nullptr, ptr<uint32_t>(c->predKeep), ptr<uint2>(c->cands), maxCands,
-                   slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches));
+                   slot(c, S_CAND_SENT), dev_err(c), c->st, &c->launches, fine_grid(c)));
   KEND(TK_PRED_EMIT);
   CK(predict_offsets(c->cfg, ptr<uint32_t>(c->pairOffsets), nPairsDev, candLocal, warpSums,
                      ptr<uint32_t>(c->candOffsets), c->st, &c->launches));

@@ -29,6 +29,24 @@ int grid_for(uint64_t items, int threads) {
   return (int)blocks;
 }
 
+// The store pass's candidates of pair gid as capture slots: slot q is the
+// hit of out[q], written as (gid, hit).
+struct CandSlots {
+  uint2* out;
+  uint32_t gid;
+  struct Ref {
+    uint2* e;
+    uint32_t gid;
+    __device__ __forceinline__ operator uint32_t() const { return e->y; }
+    __device__ __forceinline__ Ref& operator=(uint32_t v) {
+      *e = make_uint2(gid, v);
+      return *this;
+    }
+    __device__ __forceinline__ Ref& operator=(const Ref& o) { return *this = (uint32_t)o; }
+  };
+  __device__ __forceinline__ Ref operator[](uint32_t q) const { return Ref{out + q, gid}; }
+};
+
 // The count pass's walk over the fine z grid (cfg.fineRows rows per z row),
 // for windows with pL <= nP.  It visits the same hits as the walk over the
 // grid, each as often, so the counts are the same:
@@ -41,18 +59,20 @@ int grid_for(uint64_t items, int threads) {
 //    either variant's z test has zl <= z <= zh, and fine_row is monotone
 //    and keeps it in its grid row's block, so its fine row is among them.
 //    Hits outside those rows fail both z tests, as in the grid walk.
-// The captured candidates are the first predKeep store-valid visits in the
+// The captured candidates are the first nKeep store-valid visits in the
 // grid walk's order, (row, part, grid index): the visits of one (row, part)
 // come here in fine order, so the slots of the current (row, part) are kept
 // sorted by grid index -- appended while they come in order (the largest
 // is kept in a register), inserted otherwise -- and a visit past the last
-// slot replaces the largest of them when it is smaller.
-template <class Slots>
+// slot replaces the largest of them when it is smaller.  COUNT: count the
+// count variant's valid visits too (the count pass); otherwise (the store
+// pass's re-walk, both variants the store variant) stop at the first
+// (row, part) after nKeep captures, which can add nothing.
+template <bool COUNT, class Slots>
 __device__ __forceinline__ void fine_walk(const DevConfig& cfg, const PredUnionWindow& w, const FineGrid& fine,
-                                          uint32_t event, uint32_t layer, Slots slot, uint32_t& count,
-                                          uint32_t& nStore) {
+                                          uint32_t event, uint32_t layer, Slots slot, uint32_t nKeep,
+                                          uint32_t& count, uint32_t& nStore) {
   const uint32_t F = cfg.fineRows, Cf = cfg.fineC, nP = cfg.nP;
-  const uint32_t nKeep = cfg.predKeep;
   const uint32_t* lG = fine.grid + ((size_t)event * cfg.L + layer) * Cf;
   // zl, zh as pred_union_window (a switched-off variant holds +inf, -inf);
   // their grid rows are min(zLo, nZ - 1) and zHi - 1 (zHi >= 1 when any)
@@ -64,6 +84,7 @@ __device__ __forceinline__ void fine_walk(const DevConfig& cfg, const PredUnionW
   for (uint32_t r = w.zLo; r < w.zHi; ++r) {
     const uint32_t f0 = max(F * r, fLo), f1 = min(F * r + F, fHi);
     for (uint32_t part = 0; part <= w.wrap; ++part) {
+      if (!COUNT && nStore >= nKeep) return;
       const uint32_t cs = nStore;  // the first visit of this (row, part)
       uint32_t last = 0u;          // the largest kept of this (row, part), at min(nStore, nKeep) - 1
       // part 0: columns [pL, pH), or [pL, nP] under wrap; part 1: [0, pH)
@@ -78,7 +99,7 @@ __device__ __forceinline__ void fine_walk(const DevConfig& cfg, const PredUnionW
           const float4 h = __ldg(fine.hits + trax_hit(jf, cfg));  // (z, phi, grid index, 0)
           const bool lo = w.phiLow <= h.y, hi = h.y <= w.phiHigh;
           const bool phiOk = wrap ? (lo || hi) : (lo && hi);
-          count += (phiOk && zl0 <= h.x && h.x <= zh0);
+          if (COUNT) count += (phiOk && zl0 <= h.x && h.x <= zh0);
           if (phiOk && zl1 <= h.x && h.x <= zh1) {
             const uint32_t j = __float_as_uint(h.z);
             if (nStore < nKeep) {
@@ -165,7 +186,7 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
       const float zl0 = w.zLow[0], zh0 = w.zHigh[0], zl1 = w.zLow[1], zh1 = w.zHigh[1];
       const float2* zphi = reinterpret_cast<const float2*>(hits) + 1;  // (z, phi) of hit j at zphi[2 j]
       if (FINE && w.pL <= nP) {
-        fine_walk(cfg, w, fine, event, layer, slot, count, nStore);
+        fine_walk<true>(cfg, w, fine, event, layer, slot, nKeep, count, nStore);
       } else
       for (uint32_t zs = w.zLo; zs < w.zHi; ++zs) {
         uint32_t a[2], b[2];
@@ -404,14 +425,20 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 4)
 // pair has more candidates than slots.
 // At most 32 registers: full occupancy hides the latency of the dependent
 // loads better than the few spilled bytes cost (0.61 -> 0.49 ms).
-// IL: the slots' layout (keep_slots).
-template <bool IL>
-__global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
+// IL: the slots' layout (keep_slots).  FINE: the re-walks go over the fine
+// z grid (fine_walk with the store variant as both variants, its captures
+// written straight to the pair's candidates), with the same candidates; it
+// gets 40 registers, where it spills nothing (pileup batch: 4.03 ms with
+// the grid walk, 4.34 ms fine at 32 registers with 80 B spilled, 3.46 ms
+// at 40).
+template <bool IL, bool FINE>
+__global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, FINE ? 6 : 8)
     predict_store_kernel(DevConfig cfg, const uint32_t* __restrict__ grid, const float4* __restrict__ hits,
                          const uint32_t* __restrict__ hitEvt, const uint32_t* __restrict__ hitLayer,
                          const uint2* __restrict__ pairs, const uint32_t* __restrict__ nPairsDev,
                          const uint32_t* __restrict__ local, const uint32_t* __restrict__ warpStart,
-                         const uint32_t* __restrict__ keep, uint2* cands, uint32_t capCands, uint32_t* sentinels) {
+                         const uint32_t* __restrict__ keep, uint2* cands, uint32_t capCands, uint32_t* sentinels,
+                         FineGrid fine) {
   const uint32_t nPairs = *nPairsDev;
   uint32_t sent = 0;
   for (uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x; gid < nPairs; gid += gridDim.x * blockDim.x) {
@@ -442,6 +469,21 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
     const PredWindow w = pred_store_window(cfg, lt, layer, hits[hx], hits[hy]);
     uint32_t n = 0;
     const uint32_t C = cfg.C, nP = cfg.nP;
+    if (FINE && w.pL <= nP) {
+      PredUnionWindow u;
+      u.zLow[0] = u.zLow[1] = w.zLow[1];
+      u.zHigh[0] = u.zHigh[1] = w.zHigh[1];
+      u.zLo = w.zLoSec[1];
+      u.zHi = w.zHiSec[1];
+      u.phiLow = w.phiLow;
+      u.phiHigh = w.phiHigh;
+      u.pL = w.pL;
+      u.pH = w.pH;
+      u.wrap = w.wrap;
+      uint32_t unused = 0;
+      fine_walk<false>(cfg, u, fine, event, layer, CandSlots{out, gid}, limit, unused, n);
+      n = min(n, limit);
+    } else
     for (uint32_t zs = w.zLoSec[1]; zs < w.zHiSec[1] && n < limit; ++zs) {
       uint32_t a[2], b[2];
       pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
@@ -688,14 +730,18 @@ cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid,
   const bool il = keep_interleaved(cfg);
   if (emit) {
     if (maxPairs == 0) return cudaSuccess;
-    if (il)
-      predict_store_kernel<true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                             nPairsDev, candCount, warpSums, keep, cands, cap,
-                                                             sentinels);
+    if (cfg.fineRows > 0 && fine.grid)
+      predict_store_kernel<true, true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer,
+                                                                   pairs, nPairsDev, candCount, warpSums, keep,
+                                                                   cands, cap, sentinels, fine);
+    else if (il)
+      predict_store_kernel<true, false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer,
+                                                                    pairs, nPairsDev, candCount, warpSums, keep,
+                                                                    cands, cap, sentinels, fine);
     else
-      predict_store_kernel<false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
-                                                              nPairsDev, candCount, warpSums, keep, cands, cap,
-                                                              sentinels);
+      predict_store_kernel<false, false><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer,
+                                                                     pairs, nPairsDev, candCount, warpSums, keep,
+                                                                     cands, cap, sentinels, fine);
   } else if (cfg.fineRows > 0 && fine.grid) {
     predict_count_kernel<true, true><<<blocks, threads, 0, st>>>(cfg, grid, hits.xyzp, hits.evt, hits.layer, pairs,
                                                                  nPairsDev, candCount, keep, warpSums, nWarpsOut,

@@ -212,7 +212,8 @@ inline bool keep_interleaved(const DevConfig& cfg) { return cfg.predKeep >= 16u 
 // grids of up to this many cells per layer are built with shared-memory
 // counters (4 bytes per cell)
 #define TRAX_GRID_SMEM_CELLS 53248u
-// With cfg.fineRows > 0 the count pass walks `fine` (same outputs).
+// With cfg.fineRows > 0 the count pass, and the store pass's re-walks of
+// pairs with more candidates than slots, walk `fine` (same outputs).
 cudaError_t predict_pairs(const DevConfig& cfg, bool emit, const uint32_t* grid, DevHits hits, const uint2* pairs,
                           const uint32_t* nPairsDev, uint64_t maxPairs, uint32_t* candCount, uint32_t* warpSums,
                           uint32_t* nWarpsOut, uint32_t* keep, uint2* cands, uint64_t capCands,
