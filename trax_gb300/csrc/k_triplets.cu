@@ -600,17 +600,19 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 8)
     bits[lane] = 0u;
     uint32_t queued = 0;  // warp-uniform
     __syncwarp();
+    // each lane's next candidate is loaded one step ahead (0.499 -> 0.482 ms
+    // on the ttbar-like batch; its pair as well, or 40 registers, were slower)
+    uint2 cN = g0 + lane < n ? cands[g0 + lane] : make_uint2(0u, TRAX_SENTINEL);
     for (uint32_t k = 0; k < WORDS; ++k) {
       const uint32_t g = g0 + k * 32 + lane;
+      const uint2 c = cN;
+      if (k + 1 < WORDS) cN = g + 32 < n ? cands[g + 32] : make_uint2(0u, TRAX_SENTINEL);
       bool pass = false;
-      if (g < n) {
-        const uint2 c = cands[g];
-        if (c.y != TRAX_SENTINEL) {  // a slot the reference never wrote fails
-          const uint2 pr = pairs[c.x];
-          const uint32_t hx = trax_hit(pr.x, cfg);
-          pass = filter_dphi_fast(cfg, hitLayer[hx] - 1, hits[hx], hits[trax_hit(pr.y, cfg)],
-                                  hits[trax_hit(c.y, cfg)]);
-        }
+      if (c.y != TRAX_SENTINEL) {  // a slot the reference never wrote fails
+        const uint2 pr = pairs[c.x];
+        const uint32_t hx = trax_hit(pr.x, cfg);
+        pass = filter_dphi_fast(cfg, hitLayer[hx] - 1, hits[hx], hits[trax_hit(pr.y, cfg)],
+                                hits[trax_hit(c.y, cfg)]);
       }
       const uint32_t ballot = __ballot_sync(0xffffffffu, pass);
       if (pass) queue[queued + __popc(ballot & lanemask_lt())] = g;
