@@ -190,7 +190,17 @@ __global__ void __launch_bounds__(TRAX_MAX_TUNED_THREADS, 6)
       } else
       for (uint32_t zs = w.zLo; zs < w.zHi; ++zs) {
         uint32_t a[2], b[2];
-        pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
+        if (!wrap && w.pL <= nP) {
+          // pred_row_parts' result without the row's start and end: a
+          // window that does not wrap visits the columns [pL, pH) of the
+          // row (pH <= nP), and its second part is empty
+          const uint32_t row = zs * (nP + 1);
+          a[0] = cell_at(lG3, row + w.pL, C);
+          b[0] = max(a[0], cell_at(lG3, row + w.pH, C));
+          a[1] = b[1] = 0u;
+        } else {
+          pred_row_parts(w, lG3, C, nP, zs, a[0], b[0], a[1], b[1]);
+        }
 #pragma unroll
         for (int part = 0; part < 2; ++part) {
 #pragma unroll 4
