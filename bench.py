@@ -251,7 +251,7 @@ def kernel_bytes(name, st, n_tasks, n_hits, cells, cells_inner=None, cells_third
 TRAFFIC_PER_UNIT = {  # by grid (nZ x nPhi): the grid changes the cells read and the hits visited
     "150x64": {"predict_count": ("pairs", 32.5), "filter": ("candidates", 27.3), "grid_build": ("hits", 97.0)},
     "200x64": {"predict_count": ("pairs", 32.7), "filter": ("candidates", 27.3), "grid_build": ("hits", 110.9)},
-    "250x48": {"predict_count": ("pairs", 32.1), "filter": ("candidates", 30.5), "grid_build": ("hits", 107.6)},
+    "250x48": {"predict_count": ("pairs", 32.2), "filter": ("candidates", 30.5), "grid_build": ("hits", 107.6)},
     "300x48": {"predict_count": ("pairs", 32.9), "filter": ("candidates", 27.1), "grid_build": ("hits", 118.4)},
     "250x32": {"predict_count": ("pairs", 32.2), "filter": ("candidates", 27.2), "grid_build": ("hits", 90.4)},
     "200x48": {"predict_count": ("pairs", 32.4), "filter": ("candidates", 27.2), "grid_build": ("hits", 97.2)},
@@ -263,7 +263,7 @@ TRAFFIC_PER_UNIT = {  # by grid (nZ x nPhi): the grid changes the cells read and
 # 300-event capture / its units): the dominant kernels are issue-bound, so
 # their position against the SMs' issue rate is reported beside the HBM one.
 # Captured for the current prediction kernel at the workload's grid only.
-INST_PER_UNIT = {"250x48": {"predict_count": ("pairs", 24.29)}}
+INST_PER_UNIT = {"250x48": {"predict_count": ("pairs", 23.55)}}
 
 
 def kernel_issue(name, st, ms, clk, device, grid):
