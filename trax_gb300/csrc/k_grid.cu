@@ -11,7 +11,9 @@
 // slot of every hit stay in shared memory next to the counters when the
 // largest layer fits, else in global scratch.  It also writes
 // the packed (x, y, z, phi) array the candidate loops read with one 16-byte
-// load, phi being the same atan2 the cell assignment used.
+// load, phi being the same atan2 the cell assignment used.  With
+// cfg.fineRows > 0 a second kernel sorts each z row's hits again by a finer
+// z grid for the prediction count (fine_grid_kernel).
 #include <algorithm>
 
 #include "trax_kernels.h"

@@ -6,7 +6,9 @@
 // predictStore's (Q4: sqrt(x^2+y^2-tip2) vs sqrt(sqrt(x^2+y^2)^2-tip2)), the
 // store capped at the count exactly like `pos < nextThread`.  Slots the store
 // pass cannot fill (the reference leaves them unwritten) get the candidate
-// (pair, 0xffffffff), which the filter rejects.
+// (pair, 0xffffffff), which the filter rejects.  Both passes can walk a
+// finer z grid instead of the grid's rows (fine_walk, cfg.fineRows) with the
+// same results.
 //
 // The filter replaces filterCount / filterPopCount / PrefixSum / filterStore /
 // filterOffsetStore / filterOffsetMonotonizeStore (TripletThetaPhiFilter.h:50-280,
@@ -47,9 +49,10 @@ struct CandSlots {
   __device__ __forceinline__ Ref operator[](uint32_t q) const { return Ref{out + q, gid}; }
 };
 
-// The count pass's walk over the fine z grid (cfg.fineRows rows per z row),
-// for windows with pL <= nP.  It visits the same hits as the walk over the
-// grid, each as often, so the counts are the same:
+// The prediction's walk over the fine z grid (cfg.fineRows rows per z row),
+// for windows with pL <= nP, in the count pass and in the store pass's
+// re-walks.  It visits the same hits as the walk over the grid, each as
+// often, so the counts are the same:
 //  - the grid walk visits, in each z row r of [zLo, zHi), the hits of the
 //    row's phi columns [pL, pH) (no wrap), or [pL, nP] and then [0, pH)
 //    (wrap; both parts when pH > pL, so such hits twice) -- pred_row_parts
