@@ -92,6 +92,24 @@ def test_fine_rows_stage_by_stage(ctx, oracle_lib, reset):
     compare(ctx.results(), ref)
 
 
+def test_fine_grid_released_between_graph_replays(ctx, oracle_lib, reset):
+    """A graph captured with the fine grid, the grid stage run alone without
+    it (which frees the fine grid's memory), then the fine grid again: the
+    graph is captured anew instead of replayed over the freed buffers."""
+    batch = events.generate(2, n_events=4)
+    ref = oracle_lib.run(batch)[0]
+    ctx.upload(batch)
+    ctx.set_fine_rows(8)
+    ctx.seed_batch(use_graph=True)
+    compare(ctx.results(), ref)
+    ctx.set_fine_rows(0)
+    compare(stagewise(ctx, batch), ref)
+    ctx.set_fine_rows(8)
+    st = ctx.seed_batch(use_graph=True)
+    assert st.graph_captures == 1
+    compare(ctx.results(), ref)
+
+
 def test_fine_rows_on_the_full_pileup_workload(ctx, reset):
     """All 16 events of the high-occupancy workload (grid 80 x 256; the
     oracle parity of the grid walk on it is test_pileup_workload_at_full_size):

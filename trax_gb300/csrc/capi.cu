@@ -444,9 +444,10 @@ int stage_grid(trax_ctx* c, Mode mode) {
   if (c->cfg.fineRows) {
     ENSURE(fineGrid, (uint64_t)c->E * c->L * c->cfg.fineC, 4);
     ENSURE(fineHits, n, 16);
-  } else if (mode == SYNCED) {  // switched off: give its memory back
+  } else if (mode == SYNCED && (c->fineGrid.p || c->fineHits.p)) {  // switched off: give its memory back
     release(c->fineGrid);
     release(c->fineHits);
+    c->bufGeneration++;  // a captured graph that wrote them must not be replayed
   }
   GridInput in;
   in.x = ptr<float>(c->in_x);
