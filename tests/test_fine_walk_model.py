@@ -12,7 +12,9 @@ walk's because:
    test in [zl, zh] and the grid walk visits, each as often (also for
    windows across +-pi and wider than 2 pi, whose parts overlap);
 3. the captured candidates, sorted per (row, part) by grid index as they
-   arrive in fine order, are the grid walk's first ones.
+   arrive in fine order, are the grid walk's first ones, also when the
+   walk stops at the first (row, part) after the slots are full (the store
+   pass's re-walks).
 
 This file restates the grid walk (pred_row_parts), the fine walk and the
 capture's insertion and replacement rules in Python and checks the three
@@ -240,3 +242,12 @@ def test_capture_keeps_the_first_in_chunk_order():
             base = max(base + int(rng.integers(-10, 26)), 0)
         want = [j for ch in chunks for j in sorted(ch)]
         assert capture(chunks, n_keep) == (want[:n_keep], len(want))
+        # the store pass's re-walk stops at the first (row, part) that starts
+        # with n_keep captures made: what follows cannot change the slots
+        kept, total = [], 0
+        for ch in chunks:
+            if total >= n_keep:
+                break
+            kept.append(ch)
+            total += len(ch)
+        assert capture(kept, n_keep)[0] == want[:n_keep]
